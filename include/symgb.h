@@ -1,0 +1,186 @@
+/* symgb - GB300 execution engine for SymbolicLib ComputeUnit plans.
+ *
+ * C ABI of the device path.  It replaces the library that the reference's
+ * ComputeUnit::compile generates, builds with nvcc and dlopen()s
+ * (src/ComputeUnit.cpp:77-169, src/StringResources.h:15-161).  That library
+ * exports five functions over process-global state, with the plan's metadata
+ * (kernel count, instance counts, offsets, template bodies) baked into its
+ * source as globals (src/ComputeUnit.cpp:368-450).  Here the same five calls
+ * take a unit handle, and the baked-in metadata is passed once as a plan
+ * description (symgb_unit_create).  Every call returns 0 on success or a
+ * negative error code; symgb_last_error() describes the last failure on the
+ * calling thread.  No call exits the process.
+ *
+ * Plain pointers and sizes only; the library owns all device memory it
+ * allocates.  A unit is not thread-safe; distinct units are independent.
+ */
+#ifndef SYMGB_H
+#define SYMGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SYMGB_OK 0
+#define SYMGB_ERR_ARGUMENT (-1)  /* invalid argument or plan */
+#define SYMGB_ERR_CUDA (-2)      /* CUDA runtime error */
+#define SYMGB_ERR_STATE (-3)     /* call out of order (e.g. run before init) */
+#define SYMGB_ERR_TIMEOUT (-4)   /* a bounded device-side wait gave up */
+#define SYMGB_ERR_NOMEM (-5)     /* device allocation failed */
+#define SYMGB_ERR_DEVICE (-6)    /* device-side check failed (bounds) */
+
+/* Template node, post-order.  Operation codes are the reference IR's
+ * (src/Operations.hpp:9-38).  Leaves:
+ *   op = 1 (CONST): value
+ *   op = 2 (VAR):   a = id, b = group, with group
+ *       -2  output row a            (reference y[n*a + i])
+ *       -3  index variable a        (reference x[p[n*base + i] + offset], base and
+ *                                    offset from the kernel's access table)
+ *       -4  per-instance constant a (reference c[n*a + i])
+ *       253 local value a           (reference "r<a>")
+ * Inner nodes: op with nchild children (the preceding sub-trees).
+ * Statements: 24 (DEFINE local = expr), 18 (ASSIGN output = expr), 25 (BLOCK). */
+typedef struct symgb_node {
+    int32_t op;
+    int32_t nchild;
+    int32_t a;
+    int32_t b;
+    double value;
+} symgb_node;
+
+typedef struct symgb_kernel_desc {
+    uint64_t num_instances;     /* reference numInstances[k] */
+    uint64_t output_offset;     /* reference outputOffset[k] (first x slot written) */
+    uint64_t index_offset;      /* reference indexOffset[k] */
+    uint64_t constants_offset;  /* reference constantsOffset[k] */
+    uint32_t num_output_rows;
+    uint32_t num_index_rows;
+    uint32_t num_constant_rows;
+    int32_t level;              /* longest dependency path from the inputs */
+    uint32_t num_nodes;
+    const symgb_node* nodes;    /* template, post-order */
+    uint32_t num_access;
+    const int32_t* access;      /* (base row, offset) per index variable */
+} symgb_kernel_desc;
+
+typedef struct symgb_plan_desc {
+    uint32_t num_kernels;
+    const symgb_kernel_desc* kernels;  /* in execution order */
+    uint32_t num_args;
+    const uint64_t* arg_start;         /* reference argStart[] */
+    const uint64_t* arg_length;        /* reference argLength[] */
+    uint32_t num_outputs;
+    const uint64_t* output_start;      /* reference outputIndexStart[] */
+    const uint64_t* output_length;     /* reference outputIndexLength[] */
+    uint64_t num_total_memory;         /* reference numTotalMemory */
+    uint64_t num_indices;              /* reference numIndizes */
+    uint64_t num_output_values;        /* reference numOutputValues */
+    uint64_t num_constants;            /* reference numConst */
+    uint32_t threads_per_block;        /* reference Device ThreadsPerBlock */
+} symgb_plan_desc;
+
+typedef struct symgb_unit* symgb_unit_t;
+
+/* Execution schedules. */
+#define SYMGB_SCHEDULE_PLAIN 0       /* one launch per kernel, one thread per instance
+                                        and value set (the reference's run()) */
+#define SYMGB_SCHEDULE_LEVELS 1      /* one launch per dependency level, all kernels of
+                                        the level in one grid */
+#define SYMGB_SCHEDULE_PERSISTENT 2  /* one cooperative launch; levels separated by
+                                        bounded grid barriers */
+
+/* Arithmetic modes. */
+#define SYMGB_MATH_EXACT 0  /* every operation rounded separately, in template order
+                               (bit-identical to the reference without FP contraction) */
+#define SYMGB_MATH_FAST 1   /* multiply-add pairs fused into FMA */
+
+typedef struct symgb_schedule {
+    int32_t kind;               /* SYMGB_SCHEDULE_* */
+    int32_t math;               /* SYMGB_MATH_* */
+    int32_t threads_per_block;  /* 0 = plan default */
+    int32_t items_per_tile;     /* work items per CTA tile in fused schedules (0 = auto) */
+    int32_t blocks_per_sm;      /* persistent grid: CTAs per SM (0 = occupancy maximum) */
+    int32_t use_graph;          /* capture run() into a CUDA graph and replay it */
+} symgb_schedule;
+
+/* --- the reference's generated-library calls, per unit ----------------------- */
+
+/* Creates a unit from a plan description (copies it) and compiles the templates
+ * into device programs.  Replaces the plan globals of the generated source. */
+int symgb_unit_create(const symgb_plan_desc* plan, symgb_unit_t* out);
+
+/* Allocates device memory and uploads the tables.  Replaces init()
+ * (src/StringResources.h:75-123); null table pointers are an error (the
+ * reference reads its table files from the working directory instead). */
+int symgb_init(symgb_unit_t u, const uint32_t* index_data, const uint32_t* out_index_data, const double* const_data);
+
+/* Copies input container i (arg_length[i] values) from host memory.
+ * Replaces setArg (src/StringResources.h:125-127). */
+int symgb_set_arg(symgb_unit_t u, const double* d, int i);
+
+/* Evaluates all kernels and waits for completion.  Replaces run()
+ * (src/ComputeUnit.cpp:440-447). */
+int symgb_run(symgb_unit_t u);
+
+/* Copies output container k (output_length[k] values, container order) to host
+ * memory.  Replaces getResult (src/StringResources.h:129-134). */
+int symgb_get_result(symgb_unit_t u, double* d, int k);
+
+/* Replaces finish() (src/StringResources.h:136-138); releases device memory. */
+int symgb_finish(symgb_unit_t u);
+
+void symgb_unit_destroy(symgb_unit_t u);
+const char* symgb_last_error(void);
+
+/* --- schedules, value-set batches and device-resident use ------------------- */
+
+int symgb_set_schedule(symgb_unit_t u, const symgb_schedule* s);
+int symgb_get_schedule(symgb_unit_t u, symgb_schedule* s);
+
+/* Number of value sets evaluated per run (default 1).  Reallocates x. */
+int symgb_set_num_sets(symgb_unit_t u, int num_sets);
+int symgb_num_sets(symgb_unit_t u);
+
+/* Input container i for all value sets: d[set * arg_length[i] + j]. */
+int symgb_set_arg_sets(symgb_unit_t u, const double* d, int i);
+/* Output container k for all value sets: d[set * output_length[k] + j]. */
+int symgb_get_result_sets(symgb_unit_t u, double* d, int k);
+
+/* Stream used by the unit (a cudaStream_t; 0 = the unit's own stream). */
+int symgb_set_stream(symgb_unit_t u, void* stream);
+/* Enqueues the evaluation without waiting. */
+int symgb_run_async(symgb_unit_t u);
+/* Device-to-device variants: `d` is a device pointer in the same layout as the
+ * host variants; work is enqueued on the unit's stream without waiting. */
+int symgb_set_arg_sets_device(symgb_unit_t u, const double* d, int i);
+int symgb_get_result_sets_device(symgb_unit_t u, double* d, int k);
+int symgb_synchronize(symgb_unit_t u);
+
+/* Plan statistics (host side, no device needed). */
+typedef struct symgb_stats {
+    uint64_t num_kernels, num_levels;
+    uint64_t num_inputs, num_outputs, num_intermediates;
+    uint64_t index_entries, constant_entries;
+    uint64_t flops;           /* per value set: adds, muls, negations */
+    uint64_t divs, sqrts, transcendentals;
+    uint64_t gathers;         /* x reads per value set */
+    uint64_t max_registers;   /* largest per-thread register file of a kernel program */
+    uint64_t program_words;   /* total device program length (64-bit words) */
+} symgb_stats;
+int symgb_get_stats(symgb_unit_t u, symgb_stats* s);
+
+/* Algorithmic bytes of one evaluation of `num_sets` value sets:
+ * 8 N_in + 8 N_out + 16 N_int per set plus the index and constant tables once. */
+uint64_t symgb_algorithmic_bytes(symgb_unit_t u, int num_sets);
+
+/* Number of kernel launches the last run issued (graph replays count the
+ * kernels inside the graph). */
+int symgb_last_launch_count(symgb_unit_t u);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SYMGB_H */

@@ -1,0 +1,356 @@
+// Template -> device program compiler (see program.hpp).
+#include "program.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <sstream>
+#include <stdexcept>
+#include <unordered_map>
+
+namespace symgb {
+namespace engine {
+
+namespace {
+
+enum : int {
+    N_CONST = 1, N_VAR = 2, N_ADD = 3, N_MUL = 4, N_MULC = 5, N_DIV = 6, N_SQRT = 7, N_SIN = 8, N_COS = 9,
+    N_TAN = 10, N_ASIN = 12, N_ACOS = 13, N_ATAN = 14, N_EXP = 15, N_LOG = 16, N_POW = 17, N_ASSIGN = 18,
+    N_NEG = 23, N_DEFINE = 24, N_BLOCK = 25, N_REC = 26
+};
+constexpr int G_OUTPUT = -2, G_INDEX = -3, G_CONSTANT = -4, G_LOCAL = 253;
+
+struct Val {
+    int reg;
+    bool temp;  // the register may be overwritten / released by the consumer
+};
+
+class Compiler {
+public:
+    Compiler(const symgb_kernel_desc& k, int math) : k_(k), fast_(math == SYMGB_MATH_FAST) {
+        const int n = (int)k.num_nodes;
+        if (n == 0) throw std::runtime_error("empty template");
+        kids_.resize(n);
+        std::vector<int> stack;
+        for (int j = 0; j < n; ++j) {
+            const int nc = k.nodes[j].nchild;
+            if (nc < 0 || nc > (int)stack.size()) throw std::runtime_error("malformed template node list");
+            kids_[j].assign(stack.end() - nc, stack.end());
+            stack.erase(stack.end() - nc, stack.end());
+            stack.push_back(j);
+        }
+        if (stack.size() != 1) throw std::runtime_error("template is not a single tree");
+        root_ = stack.back();
+        countLocalUses(root_);
+    }
+
+    Program run() {
+        const symgb_node& r = k_.nodes[root_];
+        if (r.op == N_BLOCK) {
+            for (int s : kids_[root_]) statement(s);
+        } else {
+            statement(root_);
+        }
+        prog_.words.push_back(encode(OP_END, 0, 0, 0, 0));
+        prog_.registers = maxReg_;
+        return std::move(prog_);
+    }
+
+private:
+    const symgb_node& node(int j) const { return k_.nodes[j]; }
+
+    void countLocalUses(int j) {
+        const symgb_node& nd = node(j);
+        if (nd.op == N_VAR && nd.b == G_LOCAL) ++uses_[nd.a];
+        const bool isDef = nd.op == N_DEFINE;
+        for (std::size_t c = 0; c < kids_[j].size(); ++c) {
+            if (isDef && c == 0) continue;  // the defined name is not a use
+            countLocalUses(kids_[j][c]);
+        }
+    }
+
+    int alloc() {
+        int r;
+        if (!free_.empty()) {
+            r = free_.back();
+            free_.pop_back();
+        } else {
+            r = maxReg_++;
+            if (maxReg_ > MAX_REGISTERS) throw std::runtime_error("template needs more than 255 live values");
+        }
+        return r;
+    }
+    void release(int r) { free_.push_back(r); }
+    void consume(const Val& v) {
+        if (v.temp) release(v.reg);
+    }
+
+    void emit(std::uint64_t w) { prog_.words.push_back(w); }
+
+    // Destination for an operation on the given operands: reuse the first
+    // temporary operand register and release the other temporaries.  Sources
+    // are read before the destination is written, so reuse is safe.
+    int dstFor(std::initializer_list<Val> ops) {
+        int temps[4];
+        int nt = 0;
+        for (const Val& v : ops)
+            if (v.temp && std::find(temps, temps + nt, v.reg) == temps + nt) temps[nt++] = v.reg;
+        for (int t = 1; t < nt; ++t) release(temps[t]);
+        return nt ? temps[0] : alloc();
+    }
+
+    Val binary(int op, Val a, Val b) {
+        const int d = dstFor({a, b});
+        emit(encode(op, d, a.reg, b.reg, 0));
+        ++prog_.stats.flops;
+        return {d, true};
+    }
+
+    Val unary(int op, Val a) {
+        const int d = dstFor({a});
+        emit(encode(op, d, a.reg, 0, 0));
+        return {d, true};
+    }
+
+    Val fma(Val a, Val b, Val c, int flags) {
+        const int d = dstFor({a, b, c});
+        emit(encode(OP_FMA, d, a.reg, b.reg, (std::uint32_t)(c.reg & 0xff) | ((std::uint32_t)flags << 8)));
+        prog_.stats.flops += 2;
+        return {d, true};
+    }
+
+    bool isProduct(int j) const {
+        const symgb_node& nd = node(j);
+        return (nd.op == N_MUL && kids_[j].size() >= 2) || nd.op == N_MULC;
+    }
+
+    // Compiles all factors but the last of a product; returns (partial, last).
+    std::pair<Val, Val> productOperands(int j) {
+        const auto& ks = kids_[j];
+        Val acc = expr(ks[0]);
+        for (std::size_t c = 1; c + 1 < ks.size(); ++c) acc = binary(OP_MUL, acc, expr(ks[c]));
+        Val last = expr(ks.back());
+        return {acc, last};
+    }
+
+    Val sum(int j) {
+        const auto& ks = kids_[j];
+        if (ks.size() == 1) return expr(ks[0]);
+        bool have = false, pending = false;
+        Val acc{0, false}, pa{0, false}, pb{0, false};
+        int pflags = 0;
+        for (std::size_t c = 0; c < ks.size(); ++c) {
+            const int ch = ks[c];
+            const bool negated = node(ch).op == N_NEG;
+            const int inner = negated ? kids_[ch][0] : ch;
+            if (fast_ && isProduct(inner)) {
+                auto pr = productOperands(inner);
+                const int fl = negated ? FMA_NEG_PRODUCT : 0;
+                if (have) {
+                    acc = fma(pr.first, pr.second, acc, fl);
+                } else if (pending) {
+                    Val prev = binary(OP_MUL, pa, pb);
+                    if (pflags & FMA_NEG_PRODUCT) prev = unary(OP_NEG, prev);
+                    acc = fma(pr.first, pr.second, prev, fl);
+                    pending = false;
+                    have = true;
+                } else {
+                    pa = pr.first;
+                    pb = pr.second;
+                    pflags = fl;
+                    pending = true;
+                }
+                continue;
+            }
+            if (have && negated) {  // acc + -(e) == acc - e exactly
+                acc = binary(OP_SUB, acc, expr(inner));
+                continue;
+            }
+            Val v = expr(ch);
+            if (pending) {
+                acc = fma(pa, pb, v, pflags);
+                pending = false;
+                have = true;
+            } else if (!have) {
+                acc = v;
+                have = true;
+            } else {
+                acc = binary(OP_ADD, acc, v);
+            }
+        }
+        if (pending) {
+            acc = binary(OP_MUL, pa, pb);
+            if (pflags & FMA_NEG_PRODUCT) acc = unary(OP_NEG, acc);
+        }
+        return acc;
+    }
+
+    Val product(int j) {
+        const auto& ks = kids_[j];
+        Val acc = expr(ks[0]);
+        for (std::size_t c = 1; c < ks.size(); ++c) acc = binary(OP_MUL, acc, expr(ks[c]));
+        return acc;
+    }
+
+    Val expr(int j) {
+        const symgb_node& nd = node(j);
+        switch (nd.op) {
+            case N_CONST: {
+                const int d = alloc();
+                emit(encode(OP_LDK, d, 0, 0, 0));
+                std::uint64_t bits;
+                std::memcpy(&bits, &nd.value, 8);
+                emit(bits);
+                ++prog_.stats.constLoads;
+                return {d, true};
+            }
+            case N_VAR: {
+                if (nd.b == G_LOCAL) {
+                    auto it = regOf_.find(nd.a);
+                    if (it == regOf_.end()) throw std::runtime_error("local value used before its definition");
+                    const bool last = --uses_[nd.a] == 0;
+                    return {it->second, last};
+                }
+                const int d = alloc();
+                if (nd.b == G_INDEX) {
+                    if (nd.a < 0 || (std::uint32_t)nd.a >= k_.num_access) throw std::runtime_error("index variable out of range");
+                    const int row = k_.access[2 * nd.a], off = k_.access[2 * nd.a + 1];
+                    if (row < 0 || row > 0xffff || (std::uint32_t)row >= k_.num_index_rows)
+                        throw std::runtime_error("index row out of range");
+                    emit((std::uint64_t)OP_LDX | ((std::uint64_t)d << 8) | ((std::uint64_t)row << 16) |
+                         ((std::uint64_t)(std::uint32_t)off << 32));
+                    ++prog_.stats.gathers;
+                } else if (nd.b == G_CONSTANT) {
+                    if (nd.a < 0 || (std::uint32_t)nd.a >= k_.num_constant_rows) throw std::runtime_error("constant row out of range");
+                    emit(encode(OP_LDC, d, 0, 0, (std::uint32_t)nd.a));
+                } else {
+                    throw std::runtime_error("unsupported variable group in template");
+                }
+                return {d, true};
+            }
+            case N_ADD: return sum(j);
+            case N_MUL: return product(j);
+            case N_MULC: return product(j);
+            case N_DIV: {
+                Val a = expr(kids_[j][0]);
+                Val b = expr(kids_[j][1]);
+                Val r = binary(OP_DIV, a, b);
+                --prog_.stats.flops;
+                ++prog_.stats.divs;
+                return r;
+            }
+            case N_NEG: {
+                Val r = unary(OP_NEG, expr(kids_[j][0]));
+                ++prog_.stats.flops;
+                return r;
+            }
+            case N_SQRT: {
+                Val r = unary(OP_SQRT, expr(kids_[j][0]));
+                ++prog_.stats.sqrts;
+                return r;
+            }
+            case N_REC: {
+                Val r = unary(OP_REC, expr(kids_[j][0]));
+                ++prog_.stats.divs;
+                return r;
+            }
+            case N_POW: {
+                Val a = expr(kids_[j][0]);
+                Val b = expr(kids_[j][1]);
+                const int d = dstFor({a, b});
+                emit(encode(OP_POW, d, a.reg, b.reg, 0));
+                ++prog_.stats.transcendentals;
+                return {d, true};
+            }
+            case N_SIN: case N_COS: case N_TAN: case N_ASIN: case N_ACOS: case N_ATAN: case N_EXP: case N_LOG: {
+                static const std::unordered_map<int, int> m = {{N_SIN, OP_SIN}, {N_COS, OP_COS}, {N_TAN, OP_TAN},
+                                                               {N_ASIN, OP_ASIN}, {N_ACOS, OP_ACOS}, {N_ATAN, OP_ATAN},
+                                                               {N_EXP, OP_EXP}, {N_LOG, OP_LOG}};
+                Val r = unary(m.at(nd.op), expr(kids_[j][0]));
+                ++prog_.stats.transcendentals;
+                return r;
+            }
+            default:
+                throw std::runtime_error("operation " + std::to_string(nd.op) + " cannot be executed on the device");
+        }
+    }
+
+    void statement(int j) {
+        const symgb_node& nd = node(j);
+        if (nd.op == N_BLOCK) {  // nested statement list
+            for (int s : kids_[j]) statement(s);
+        } else if (nd.op == N_DEFINE) {
+            const symgb_node& name = node(kids_[j][0]);
+            if (name.op != N_VAR || name.b != G_LOCAL) throw std::runtime_error("DEFINE of a non-local");
+            Val v = expr(kids_[j][1]);
+            if (uses_[name.a] == 0) {  // defined but never read
+                consume(v);
+                return;
+            }
+            if (!v.temp) {  // alias of another live local: copy
+                const int d = alloc();
+                emit(encode(OP_MOV, d, v.reg, 0, 0));
+                v = {d, true};
+            }
+            regOf_[name.a] = v.reg;
+        } else if (nd.op == N_ASSIGN) {
+            const symgb_node& out = node(kids_[j][0]);
+            if (out.op != N_VAR || out.b != G_OUTPUT) throw std::runtime_error("ASSIGN to a non-output");
+            if (out.a < 0 || (std::uint32_t)out.a >= k_.num_output_rows) throw std::runtime_error("output row out of range");
+            Val v = expr(kids_[j][1]);
+            emit(encode(OP_ST, 0, v.reg, 0, (std::uint32_t)out.a));
+            ++prog_.stats.stores;
+            consume(v);
+        } else {
+            throw std::runtime_error("template statement is neither DEFINE nor ASSIGN");
+        }
+    }
+
+    const symgb_kernel_desc& k_;
+    bool fast_;
+    std::vector<std::vector<int>> kids_;
+    int root_ = 0;
+    std::unordered_map<int, int> uses_, regOf_;
+    std::vector<int> free_;
+    int maxReg_ = 0;
+    Program prog_;
+};
+
+}  // namespace
+
+Program compileTemplate(const symgb_kernel_desc& k, int math) {
+    Compiler c(k, math);
+    return c.run();
+}
+
+std::string disassemble(const Program& p) {
+    static const char* names[NUM_OPCODES] = {"end", "ldx", "ldc", "ldk", "st", "add", "sub", "mul", "div", "neg", "sqrt",
+                                             "rec", "fma", "sin", "cos", "tan", "asin", "acos", "atan", "exp", "log",
+                                             "pow", "mov"};
+    std::ostringstream os;
+    for (std::size_t pc = 0; pc < p.words.size(); ++pc) {
+        const std::uint64_t w = p.words[pc];
+        const int op = (int)(w & 0xff), d = (int)((w >> 8) & 0xff), a = (int)((w >> 16) & 0xff),
+                  b = (int)((w >> 24) & 0xff);
+        const std::int32_t imm = (std::int32_t)(w >> 32);
+        os << (op < NUM_OPCODES ? names[op] : "?") << " ";
+        switch (op) {
+            case OP_LDX: os << "r" << d << " row" << ((w >> 16) & 0xffff) << " off" << imm; break;
+            case OP_LDC: os << "r" << d << " crow" << imm; break;
+            case OP_LDK: {
+                double v;
+                std::memcpy(&v, &p.words[pc + 1], 8);
+                os << "r" << d << " " << v;
+                ++pc;
+                break;
+            }
+            case OP_ST: os << "y" << imm << " r" << a; break;
+            case OP_FMA: os << "r" << d << " r" << a << " r" << b << " r" << (imm & 0xff) << " f" << (imm >> 8); break;
+            default: os << "r" << d << " r" << a << " r" << b;
+        }
+        os << "\n";
+    }
+    return os.str();
+}
+
+}  // namespace engine
+}  // namespace symgb

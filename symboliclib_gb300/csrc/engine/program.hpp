@@ -1,0 +1,78 @@
+// Device programs: the form in which the engine's interpreter kernels execute
+// a ComputeKernel template.
+//
+// A template (post-order nodes of a BLOCK of DEFINE / ASSIGN statements) is
+// compiled into a linear sequence of 64-bit instructions over a per-thread
+// register file.  Every thread runs the same program for its own instance and
+// value set, so instruction fetch and decode are warp-uniform.  In exact mode
+// each template operation is one rounded operation in the template's order
+// (n-ary sums and products left to right, as C evaluates the reference's
+// generated code), so results are bit-identical to the reference compiled
+// without FP contraction.  In fast mode, products feeding a sum are fused into
+// FMA.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "symgb.h"
+
+namespace symgb {
+namespace engine {
+
+// Instruction word: op (bits 0-7), dst (8-15), a (16-23), b (24-31), imm (32-63).
+enum Opcode : std::uint8_t {
+    OP_END = 0,
+    OP_LDX = 1,   // r[dst] = x[p[row * n + i] + off]; row = bits 16-31, off = imm (signed)
+    OP_LDC = 2,   // r[dst] = c[row * n + i]; row = imm
+    OP_LDK = 3,   // r[dst] = next word as double
+    OP_ST = 4,    // y[row * n + i] = r[a]; row = imm
+    OP_ADD = 5,
+    OP_SUB = 6,   // r[a] - r[b]  (== r[a] + -(r[b]) exactly)
+    OP_MUL = 7,
+    OP_DIV = 8,
+    OP_NEG = 9,
+    OP_SQRT = 10,
+    OP_REC = 11,  // 1 / r[a]
+    OP_FMA = 12,  // r[dst] = (+-)(r[a] * r[b]) (+-) r[c]; c = bits 32-39, flags bits 40-41
+    OP_SIN = 13,
+    OP_COS = 14,
+    OP_TAN = 15,
+    OP_ASIN = 16,
+    OP_ACOS = 17,
+    OP_ATAN = 18,
+    OP_EXP = 19,
+    OP_LOG = 20,
+    OP_POW = 21,
+    OP_MOV = 22,
+    NUM_OPCODES
+};
+
+constexpr int FMA_NEG_PRODUCT = 1;
+constexpr int FMA_NEG_ADDEND = 2;
+constexpr int MAX_REGISTERS = 255;
+
+struct ProgramStats {
+    std::uint64_t flops = 0, divs = 0, sqrts = 0, transcendentals = 0, gathers = 0, constLoads = 0, stores = 0;
+};
+
+struct Program {
+    std::vector<std::uint64_t> words;
+    int registers = 0;
+    ProgramStats stats;
+};
+
+// Compiles one kernel template.  Throws std::runtime_error on templates the
+// engine cannot execute (unknown operations, more than MAX_REGISTERS live values).
+Program compileTemplate(const symgb_kernel_desc& k, int math);
+
+// Human-readable listing (tests and debugging).
+std::string disassemble(const Program& p);
+
+inline std::uint64_t encode(int op, int dst, int a, int b, std::uint32_t imm) {
+    return (std::uint64_t)(op & 0xff) | ((std::uint64_t)(dst & 0xff) << 8) | ((std::uint64_t)(a & 0xff) << 16) |
+           ((std::uint64_t)(b & 0xff) << 24) | ((std::uint64_t)imm << 32);
+}
+
+}  // namespace engine
+}  // namespace symgb

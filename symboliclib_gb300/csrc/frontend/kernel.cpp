@@ -1,0 +1,220 @@
+// ComputeKernel: one template expression applied over per-instance tables.
+//
+// Restates reference src/ComputeKernel.cpp:27-484.  The instances of a group
+// are walked in lockstep; wherever the instances differ only in a leaf, the
+// leaf becomes a table row: output variables (group -2), variables read through
+// the index table (group -3) and per-instance constants (group -4).  The
+// template is then rewritten (constant folding, local common-sub-expression
+// extraction into DEFINE statements, simplification) and its statements are
+// put into dependency order.
+#include <map>
+#include <unordered_set>
+
+#include "symgb/frontend.hpp"
+#include "symgb/traverse.hpp"
+
+namespace symgb {
+
+namespace {
+
+hash_t hashInstances(const std::vector<Symbolic>& x) {
+    std::vector<hash_t> hs;
+    hs.reserve(x.size());
+    for (auto& xi : x) hs.push_back(xi.ahash());
+    return hashVector(hs);
+}
+
+// The lockstep cursor: the same child position across all instances.
+struct Lockstep {
+    std::vector<Symbolic> x;
+    hash_t h = 0;
+    unsigned childCounter = 0;
+
+    explicit Lockstep(const std::vector<Symbolic>& xs) : x(xs) { init(); }
+    Lockstep(const std::vector<Symbolic>& parents, unsigned child) {
+        x.reserve(parents.size());
+        for (auto& p : parents) x.push_back(p[child]);
+        init();
+    }
+    void init() {
+        if (!x.empty()) h = hashInstances(x);
+    }
+    unsigned numChilds() const { return x.empty() ? 0 : x.front().numChilds(); }
+    OpType op() const { return x.empty() ? NOOP : x.front().op(); }
+    bool visit() { return childCounter++ == x.front().numChilds(); }
+
+    // The variable of every instance.  The table is never collapsed to a single
+    // entry: the reference's all-identical test (ComputeKernel.cpp:92) is
+    // inverted and always fails.
+    std::vector<std::array<int, 2>> variables() const {
+        std::vector<std::array<int, 2>> v(x.size());
+        for (std::size_t i = 0; i < x.size(); ++i) v[i] = x[i].variable();
+        return v;
+    }
+    // The constant of every instance, or one value if all are equal.
+    std::vector<double> constants() const {
+        std::vector<double> v(x.size());
+        bool allEqual = true;
+        for (std::size_t i = 0; i < x.size(); ++i) {
+            v[i] = x[i].constant();
+            if (allEqual && v[0] != v[i]) allEqual = false;
+        }
+        if (allEqual) v.resize(1);
+        return v;
+    }
+};
+
+}  // namespace
+
+ComputeKernel::ComputeKernel(const std::vector<Symbolic>& instances, int simdWidth)
+    : n_(instances.size()), simdWidth_(simdWidth) {
+    std::map<hash_t, Symbolic> seen;  // instance-list hash -> template sub-tree
+    std::vector<Lockstep> stack;
+    stack.emplace_back(instances);
+    std::vector<Symbolic> built;
+
+    while (!stack.empty()) {
+        Lockstep& cur = stack.back();
+        if (cur.visit()) {
+            const unsigned nc = cur.numChilds();
+            Symbolic t(cur.op(), std::vector<Symbolic>(built.end() - nc, built.end()));
+            built.erase(built.end() - nc, built.end());
+            built.push_back(t);
+            if (seen.find(cur.h) == seen.end()) seen[cur.h] = t;
+            stack.pop_back();
+            continue;
+        }
+        const OpType parentOp = cur.op();
+        const unsigned childPos = cur.childCounter;  // 1-based position of this child
+        Lockstep data(cur.x, childPos - 1);
+        auto it = seen.find(data.h);
+        if (it != seen.end()) {
+            built.push_back(it->second);
+        } else if (data.op() == VAR) {
+            auto values = data.variables();
+            if (parentOp == ASSIGN && childPos == 1) {
+                built.push_back(Symbolic((int)outputTable_.size(), TEMPLATE_OUTPUT));
+                outputTable_.push_back(std::move(values));
+            } else {
+                built.push_back(Symbolic((int)variableTable_.size(), TEMPLATE_INDEX));
+                variableTable_.push_back(std::move(values));
+            }
+            seen[data.h] = built.back();
+        } else if (data.op() == CONST) {
+            auto values = data.constants();
+            if (values.size() == 1) {
+                built.push_back(Symbolic(values.front()));
+            } else {
+                built.push_back(Symbolic((int)constantTable_.size(), TEMPLATE_CONSTANT));
+                constantTable_.push_back(std::move(values));
+            }
+            seen[data.h] = built.back();
+        } else {
+            stack.push_back(std::move(data));  // invalidates `cur`
+        }
+    }
+
+    // Pad to a multiple of the SIMD width (reference ComputeKernel.cpp:241-259).
+    if (simdWidth_ > 1 && n_ > (std::size_t)simdWidth_ && n_ % simdWidth_) {
+        const std::size_t pad = simdWidth_ - n_ % simdWidth_;
+        for (auto& c : constantTable_) c.insert(c.end(), pad, 0.0);
+        for (auto& v : variableTable_) {
+            const std::array<int, 2> last = v.back();
+            v.insert(v.end(), pad, last);
+        }
+        for (auto& v : outputTable_) v.insert(v.end(), pad, std::array<int, 2>{-1, -1});
+        n_ += pad;
+    }
+
+    assert(built.size() == 1);
+    template_ = built.front();
+    optimizeTemplate();
+}
+
+// Reference ComputeKernel.cpp:270-323.
+void ComputeKernel::optimizeTemplate() {
+    template_ = removeConstantExpressions(template_);
+    template_ = removeConstantExpressions(template_);
+    template_ = referenceRedundant(template_);
+
+    std::vector<ExpressionBlock> blocks = decompose({template_}, 0, LOCAL_VAR, false);
+    for (auto& b : blocks) b.x = simplify(b.x);
+    for (auto& b : blocks)
+        if (b.x.op() == ASSIGN && b.x[0].variable()[1] == LOCAL_VAR) b.x = Symbolic(DEFINE, b.x[0], b.x[1]);
+
+    std::vector<std::unordered_set<int>> graph(blocks.size());
+    for (int i = 0; i < (int)blocks.size(); ++i)
+        for (int c : blocks[i].childs) graph[c].insert(i);
+    std::vector<int> order = topologicalOrder(graph);
+    std::vector<Symbolic> statements;
+    for (int i : order) statements.push_back(blocks[i].x);
+    template_ = Symbolic(BLOCK, statements);
+}
+
+const std::vector<std::array<int, 2>>& ComputeKernel::outputVariableData() {
+    if (outputData_.empty()) outputPack_ = appendTransposed(outputTable_, outputData_, simdWidth_);
+    return outputData_;
+}
+
+const std::vector<double>& ComputeKernel::constantData() {
+    if (constantData_.empty()) constantsPack_ = appendTransposed(constantTable_, constantData_, simdWidth_);
+    return constantData_;
+}
+
+const std::vector<std::array<int, 2>>& ComputeKernel::variableData() {
+    if (variableData_.empty()) {
+        findCorrelatedVariables();
+        variablePack_ = appendTransposed(variableTable_, variableData_, simdWidth_);
+    }
+    return variableData_;
+}
+
+// Index rows whose entries differ from an earlier row by one constant offset
+// (same input group, same relative pattern) share that row; the template reads
+// them as x[p[base] + offset] (reference ComputeKernel.cpp:413-484).
+void ComputeKernel::findCorrelatedVariables() {
+    std::map<hash_t, int> patterns;
+    int i = 0;
+    for (auto& vars : variableTable_) {
+        std::vector<int> vals;
+        bool sameGroup = true;
+        vals.push_back(vars[0][1]);
+        for (auto& v : vars) {
+            if (v[1] != vars[0][1]) {
+                sameGroup = false;
+                break;
+            }
+            vals.push_back(v[0] - vars[0][0]);
+        }
+        if (!sameGroup || vars[0][1] == GLOBAL_INTERMEDIATE || vars[0][1] == EXPLICIT_INTERMEDIATE) {
+            access_.push_back({i, 0});
+        } else {
+            const hash_t h = hashVector(vals);
+            auto it = patterns.find(h);
+            if (it == patterns.end()) {
+                patterns[h] = i;
+                access_.push_back({i, 0});
+            } else {
+                access_.push_back({it->second, vars[0][0] - variableTable_[it->second][0][0]});
+            }
+        }
+        ++i;
+    }
+    // Keep only the rows that are read explicitly, renumbered densely.
+    std::map<int, int> kept;
+    std::vector<std::vector<std::array<int, 2>>> table;
+    int next = 0;
+    for (auto& a : access_) {
+        auto it = kept.find(a.baseRow);
+        if (it == kept.end()) {
+            kept[a.baseRow] = next;
+            table.push_back(variableTable_[a.baseRow]);
+            a.baseRow = next++;
+        } else {
+            a.baseRow = it->second;
+        }
+    }
+    variableTable_.swap(table);
+}
+
+}  // namespace symgb

@@ -1,0 +1,228 @@
+// ComputeUnit planning: containers -> decomposition -> kernels -> execution
+// order -> memory layout and tables (reference src/ComputeUnit.cpp:172-451).
+#include <cstring>
+#include <iomanip>
+#include <map>
+#include <set>
+#include <sstream>
+#include <stdexcept>
+#include <unordered_map>
+
+#include "symgb/frontend.hpp"
+#include "symgb/traverse.hpp"
+
+namespace symgb {
+
+// A container whose entries are all variables is an input: they must be
+// VAR(0..len-1, g) of one group g.  Any other container holds outputs, each
+// wrapped as ASSIGN(VAR(i, -10 - k), expr) for the k-th output container
+// (reference ComputeUnit.cpp:172-228).
+void PlanBuilder::addContainer(const Symbolic* expr, std::size_t len) {
+    if (!len) return;
+    bool isInput = true;
+    for (std::size_t i = 0; i < len; ++i)
+        if (expr[i].op() != VAR) {
+            isInput = false;
+            break;
+        }
+    if (isInput) {
+        const int group = expr[0].variable()[1];
+        for (std::size_t i = 0; i < len; ++i) {
+            if (expr[i].variable()[0] != (int)i) throw std::invalid_argument("input variables are not numbered 0..n-1 in order");
+            if (expr[i].variable()[1] != group) throw std::invalid_argument("input container mixes variable groups");
+        }
+        inputSizes_.push_back(len);
+        inputOffsets_.emplace_back(group, inputDataSize_);
+        inputDataSize_ += len;
+    } else {
+        for (std::size_t i = 0; i < len; ++i)
+            outputExpressions_.emplace_back(ASSIGN, Symbolic((int)i, -10 - outputCount_), expr[i]);
+        outputIds_.push_back(std::vector<int>(len, -1));
+        ++outputCount_;
+    }
+}
+
+Plan PlanBuilder::build() {
+    Plan& P = plan_;
+    const DeviceConfig& dev = P.device;
+    std::vector<ExpressionBlock> blocks =
+        decompose(outputExpressions_, (unsigned char)dev.decompositionThreshold, GLOBAL_INTERMEDIATE, true);
+
+    // Group blocks by (structure hash, level) in first-seen order (ComputeUnit.cpp:34-56).
+    std::unordered_map<hash_t, int> groupMap;
+    std::vector<std::vector<int>> groups;
+    for (int i = 0; i < (int)blocks.size(); ++i) {
+        const hash_t h = hashPair(blocks[i].structureHash, blocks[i].level);
+        int& id = groupMap[h];
+        if (id) {
+            groups[id - 1].push_back(i);
+        } else {
+            groups.push_back({i});
+            id = (int)groups.size();
+        }
+    }
+    std::vector<int> blockGroup(blocks.size());
+    std::vector<ComputeKernel> kernels;
+    kernels.reserve(groups.size());
+    for (int g = 0; g < (int)groups.size(); ++g) {
+        std::vector<Symbolic> inst(groups[g].size());
+        for (std::size_t j = 0; j < groups[g].size(); ++j) {
+            inst[j] = blocks[groups[g][j]].x;
+            blockGroup[groups[g][j]] = g;
+        }
+        int width;
+        if (dev.vectorWidth == 0)
+            width = 0;
+        else if (inst.size() > dev.vectorWidth)
+            width = (int)dev.vectorWidth;
+        else
+            width = 1;
+        kernels.emplace_back(inst, width);
+    }
+
+    // Execution order: children before parents (ComputeUnit.cpp:279-296).
+    std::vector<std::set<int>> deps(kernels.size());
+    for (int i = 0; i < (int)blocks.size(); ++i)
+        for (int j : blocks[i].childs)
+            if (j != -1) deps[blockGroup[j]].insert(blockGroup[i]);
+    std::vector<int> order = topologicalOrder(deps);
+    if (order.size() != kernels.size()) throw std::runtime_error("kernel dependency graph has a cycle");
+
+    // Longest-path level of every kernel (0 = reads only inputs).
+    std::vector<int> levelOf(kernels.size(), 0);
+    for (int k : order)
+        for (int parent : deps[k]) levelOf[parent] = std::max(levelOf[parent], levelOf[k] + 1);
+
+    P.kernels.clear();
+    P.kernels.reserve(kernels.size());
+    for (int k : order) {
+        P.kernels.push_back(std::move(kernels[k]));
+        P.kernelLevel.push_back(levelOf[k]);
+    }
+
+    // Memory layout: x = [inputs | output and intermediate slots in kernel order].
+    std::size_t variableDataSize = 0;
+    std::unordered_map<hash_t, std::size_t> intermediatePositions;
+    for (auto& k : P.kernels) {
+        k.outputOffset = inputDataSize_ + variableDataSize;
+        for (auto var : k.outputVariableData()) {
+            if (var[1] <= -10) {
+                outputIds_[-(10 + var[1])][var[0]] = (int)(inputDataSize_ + variableDataSize++);
+            } else {
+                if (var[0] != -1) intermediatePositions[hashVariable(var)] = variableDataSize;
+                ++variableDataSize;
+            }
+        }
+    }
+    for (auto& ids : outputIds_) P.outputIdsFlat.insert(P.outputIdsFlat.end(), ids.begin(), ids.end());
+
+    for (auto& k : P.kernels) {
+        k.constantsOffset = P.constantData.size();
+        const auto& cd = k.constantData();
+        P.constantData.insert(P.constantData.end(), cd.begin(), cd.end());
+    }
+
+    std::map<int, std::size_t> inputOffsets(inputOffsets_.begin(), inputOffsets_.end());
+    for (auto& k : P.kernels) {
+        k.indexOffset = P.positionData.size();
+        for (auto& x : k.variableData()) {
+            if (x[1] == GLOBAL_INTERMEDIATE || x[1] == EXPLICIT_INTERMEDIATE) {
+                auto it = intermediatePositions.find(hashVariable(x));
+                if (it == intermediatePositions.end()) throw std::runtime_error("intermediate read before it is produced");
+                P.positionData.push_back((unsigned)(inputDataSize_ + it->second));
+            } else {
+                P.positionData.push_back((unsigned)(inputOffsets[x[1]] + x[0]));
+            }
+        }
+    }
+
+    std::size_t acc = 0;
+    for (std::size_t s : inputSizes_) {
+        P.argStart.push_back(acc);
+        P.argLength.push_back(s);
+        acc += s;
+    }
+    acc = 0;
+    for (auto& ids : outputIds_) {
+        P.outputIndexStart.push_back(acc);
+        P.outputIndexLength.push_back(ids.size());
+        acc += ids.size();
+    }
+    P.inputDataSize = inputDataSize_;
+    P.numTotalMemory = inputDataSize_ + variableDataSize;
+    return std::move(plan_);
+}
+
+namespace {
+
+const char* opName(OpType op) {
+    static const char* names[NUM_OPS] = {"NOOP", "CONST", "VAR", "ADD", "MUL", "MULC", "DIV", "SQRT", "SIN", "COS",
+                                         "TAN", "COT", "ASIN", "ACOS", "ATAN", "EXP", "LOG", "POW", "ASSIGN", "GROUP",
+                                         "CONDPOS", "CONDNONZERO", "CONDZERO", "NEG", "DEFINE", "BLOCK", "REC",
+                                         "FIXED", "FUNC", "CALL"};
+    return op < NUM_OPS ? names[op] : "?";
+}
+
+void writeTemplate(const Symbolic& x, std::ostream& os) {
+    switch (x.op()) {
+        case CONST: {
+            std::uint64_t bits;
+            double c = x.constant();
+            std::memcpy(&bits, &c, 8);
+            os << "#" << std::hex << bits << std::dec;
+            return;
+        }
+        case VAR: os << "v(" << x.variable()[0] << "," << x.variable()[1] << ")"; return;
+        default:
+            os << "(" << opName(x.op());
+            for (auto& c : x) {
+                os << " ";
+                writeTemplate(c, os);
+            }
+            os << ")";
+    }
+}
+
+template <class T>
+void writeList(std::ostream& os, const char* name, const std::vector<T>& v) {
+    os << name << " " << v.size() << ":";
+    for (auto& e : v) os << " " << e;
+    os << "\n";
+}
+
+}  // namespace
+
+std::string templateText(const Symbolic& t) {
+    std::ostringstream os;
+    writeTemplate(t, os);
+    return os.str();
+}
+
+void dumpPlan(Plan& P, std::ostream& os) {
+    os << "kernels " << P.kernels.size() << "\n";
+    for (std::size_t k = 0; k < P.kernels.size(); ++k) {
+        auto& K = P.kernels[k];
+        os << "kernel " << k << " n=" << K.numInstances() << " outOff=" << K.outputOffset << " idxOff=" << K.indexOffset
+           << " constOff=" << K.constantsOffset << "\n";
+        os << "access";
+        for (auto& a : K.access()) os << " " << a.baseRow << ":" << a.offset;
+        os << "\n";
+        os << "template " << templateText(K.templateExpression()) << "\n";
+    }
+    writeList(os, "argStart", P.argStart);
+    writeList(os, "argLength", P.argLength);
+    writeList(os, "outputIndexStart", P.outputIndexStart);
+    writeList(os, "outputIndexLength", P.outputIndexLength);
+    os << "numTotalMemory " << P.numTotalMemory << "\n";
+    writeList(os, "positionData", P.positionData);
+    writeList(os, "outputIds", P.outputIdsFlat);
+    os << "constantData " << P.constantData.size() << ":";
+    for (double c : P.constantData) {
+        std::uint64_t bits;
+        std::memcpy(&bits, &c, 8);
+        os << " " << std::hex << bits << std::dec;
+    }
+    os << "\n";
+}
+
+}  // namespace symgb

@@ -1,0 +1,271 @@
+// Symbolic node construction, hashing and arithmetic.
+#include "symgb/symbolic.hpp"
+
+#include <algorithm>
+#include <atomic>
+#include <cstdlib>
+#include <mutex>
+
+#include "symgb/traverse.hpp"
+
+namespace symgb {
+
+namespace {
+
+// Reflected CRC-64 table of the Jones polynomial (0xad93d23594c935a9, bit
+// reversed 0x95ac9329ac4bc9b5), generated rather than written out.
+struct Crc64Table {
+    std::uint64_t t[256];
+    Crc64Table() {
+        const std::uint64_t poly = 0x95ac9329ac4bc9b5ULL;
+        for (int i = 0; i < 256; ++i) {
+            std::uint64_t c = (std::uint64_t)i;
+            for (int k = 0; k < 8; ++k) c = (c & 1) ? (c >> 1) ^ poly : (c >> 1);
+            t[i] = c;
+        }
+    }
+};
+
+std::atomic<long long> g_liveNodes{0};
+
+// Nodes are small and created by the million; a per-thread free list keeps
+// allocation off the general-purpose heap.
+struct NodePool {
+    std::vector<Symbolic::Node*> freeList;
+    Symbolic::Node* get() {
+        if (freeList.empty()) {
+            const std::size_t n = 4096;
+            auto* slab = static_cast<Symbolic::Node*>(std::malloc(n * sizeof(Symbolic::Node)));
+            for (std::size_t i = 0; i < n; ++i) freeList.push_back(slab + (n - 1 - i));
+        }
+        Symbolic::Node* p = freeList.back();
+        freeList.pop_back();
+        return p;
+    }
+    void put(Symbolic::Node* p) { freeList.push_back(p); }
+};
+
+// One global pool guarded by a mutex would serialise the front end; nodes are
+// instead returned to the free list of the thread that frees them.  Slabs are
+// never returned to the heap, so a node may be freed by any thread and handles
+// with static storage duration stay valid until exit.
+NodePool& pool() {
+    static thread_local NodePool p;
+    return p;
+}
+
+}  // namespace
+
+const std::uint64_t* crc64Table() {
+    static const Crc64Table table;
+    return table.t;
+}
+
+long long liveNodeCount() { return g_liveNodes.load(); }
+
+int& Symbolic::uniqueVariableCounter() {
+    static int counter = 0;
+    return counter;
+}
+
+Symbolic Symbolic::generateUniqueVariable() {
+    return Symbolic(uniqueVariableCounter()++, EXPLICIT_INTERMEDIATE);
+}
+
+Symbolic::Node* Symbolic::allocate(OpType op, unsigned numChilds) {
+    Node* n = pool().get();
+    n->ref = 1;
+    n->op = op;
+    n->complexity = 0;
+    n->numChilds = numChilds;
+    n->algebraicHash = 0;
+    n->childs = nullptr;
+    ++g_liveNodes;
+    return n;
+}
+
+void Symbolic::release() {
+    if (data && --data->ref == 0) {
+        if (data->op != CONST && data->op != VAR && data->numChilds) delete[] data->childs;
+        pool().put(data);
+        --g_liveNodes;
+    }
+    data = nullptr;
+}
+
+Symbolic::Symbolic(double c) {
+    data = allocate(CONST, 0);
+    data->constant = c;
+    finish();
+}
+
+Symbolic::Symbolic(int id, int group) {
+    data = allocate(VAR, 0);
+    data->variable = {id, group};
+    finish();
+}
+
+Symbolic::Symbolic(OpType op, const Symbolic& c0) {
+    data = allocate(op, 1);
+    data->childs = new Symbolic[1]{c0};
+    finish();
+}
+
+Symbolic::Symbolic(OpType op, const Symbolic& c0, const Symbolic& c1) {
+    data = allocate(op, 2);
+    data->childs = new Symbolic[2]{c0, c1};
+    finish();
+}
+
+Symbolic::Symbolic(OpType op, const std::vector<Symbolic>& childs) {
+    data = allocate(op, (unsigned)childs.size());
+    if (!childs.empty()) {
+        data->childs = new Symbolic[childs.size()];
+        std::copy(childs.begin(), childs.end(), data->childs);
+    }
+    finish();
+}
+
+Symbolic::Symbolic(OpType op, Symbolic* childs, unsigned n) {
+    data = allocate(op, n);
+    data->childs = n ? childs : nullptr;
+    if (!n) delete[] childs;
+    finish();
+}
+
+// Algebraic hash (reference Symbolic.cpp:61-116): sums and products combine
+// child hashes commutatively (wrapping integer + and *), constants hash to their
+// integer value when integral, everything else chains CRC hashes.
+void Symbolic::finish() {
+    Node& d = *data;
+    const unsigned n = d.numChilds;
+    const Symbolic* ch = (d.op == CONST || d.op == VAR) ? nullptr : d.childs;
+    std::uint64_t h = 0;
+    bool done = false;
+    switch (d.op) {
+        case MUL:
+        case MULC:
+            h = 1;
+            for (unsigned i = 0; i < n; ++i) {
+                const std::uint64_t ci = ch[i].op() == ADD ? (std::uint64_t)hashPair(opInfo(ADD).seed, ch[i].ahash())
+                                                           : (std::uint64_t)ch[i].ahash();
+                h *= ci;
+            }
+            break;
+        case ADD:
+            h = 0;
+            for (unsigned i = 0; i < n; ++i) {
+                const std::uint64_t ci = (ch[i].op() == MUL || ch[i].op() == MULC)
+                                             ? (std::uint64_t)hashPair(opInfo(MUL).seed, ch[i].ahash())
+                                             : (std::uint64_t)ch[i].ahash();
+                h += ci;
+            }
+            break;
+        case CONST: {
+            const double c = d.constant;
+            if (c == 0.0) {
+                h = 0;
+            } else if (c == (double)(hash_t)c) {
+                h = (std::uint64_t)(hash_t)c;
+            } else {
+                h = (std::uint64_t)hashValue(c);
+            }
+            break;
+        }
+        case VAR:
+            h = (std::uint64_t)hashPair(opInfo(VAR).seed, hashVariable(d.variable));
+            break;
+        default:
+            if (d.op == DIV) {
+                if (ch[0].ahash() == 0) {
+                    h = 0;
+                    done = true;
+                } else if (ch[0].ahash() == ch[1].ahash()) {
+                    h = 1;
+                    done = true;
+                }
+            }
+            if (!done) {
+                hash_t hh = opInfo(d.op).seed;
+                for (unsigned i = 0; i < n; ++i) {
+                    const OpType opi = ch[i].op();
+                    if (opi == MULC || opi == MUL || opi == ADD)
+                        hh = hashPair(hh, hashPair(opInfo(opi).seed, ch[i].ahash()));
+                    else
+                        hh = hashPair(hh, ch[i].ahash());
+                }
+                h = (std::uint64_t)hh;
+            }
+    }
+    d.algebraicHash = (hash_t)h;
+
+    // Complexity (reference Symbolic.cpp:119-131), saturating at 255.
+    if (!n || d.op == CONST || d.op == VAR) {
+        d.complexity = opInfo(d.op).cost;
+    } else {
+        unsigned tmp = 0;
+        for (unsigned i = 0; i < n; ++i) tmp += ch[i].complexity();
+        d.complexity = (std::uint8_t)std::min(255u, n * opInfo(d.op).cost + tmp);
+    }
+}
+
+// Structure hash: post-order CRC chain of child structure hashes and the
+// operation seed; leaves hash to their seed (reference Symbolic.cpp:168-174).
+hash_t Symbolic::computeStructureHash() const {
+    return traverseGenerateIdentity<hash_t>(*this, [](const Symbolic& x, const std::vector<hash_t>& hs) {
+        if (hs.empty()) return opInfo(x.op()).seed;
+        std::vector<hash_t> all(hs);
+        all.push_back(opInfo(x.op()).seed);
+        return hashVector(all);
+    });
+}
+
+Symbolic operator*(const Symbolic& a, const Symbolic& b) {
+    if (a.op() == CONST) return Symbolic(MULC, a, b);
+    if (b.op() == CONST) return Symbolic(MULC, b, a);
+    return Symbolic(MUL, a, b);
+}
+
+Symbolic operator+(const Symbolic& a, const Symbolic& b) { return Symbolic(ADD, a, b); }
+
+Symbolic operator/(const Symbolic& a, const Symbolic& b) { return Symbolic(DIV, a, b); }
+
+Symbolic operator-(const Symbolic& a, const Symbolic& b) {
+    return Symbolic(ADD, a, Symbolic(MULC, Symbolic(-1.0), b));
+}
+
+Symbolic operator-(const Symbolic& a) { return Symbolic(MULC, Symbolic(-1.0), a); }
+
+Symbolic sqrt(const Symbolic& a) { return Symbolic(SQRT, a); }
+
+double evaluateOp(OpType op, const double* v, unsigned n) {
+    switch (op) {
+        case ADD: {
+            double r = 0.0;
+            for (unsigned i = 0; i < n; ++i) r += v[i];
+            return r;
+        }
+        case MUL: {
+            double r = 1.0;
+            for (unsigned i = 0; i < n; ++i) r *= v[i];
+            return r;
+        }
+        case MULC: return v[0] * v[1];
+        case DIV: return v[0] / v[1];
+        case SQRT: return std::sqrt(v[0]);
+        case NEG: return -v[0];
+        case RECIPROCAL: return 1.0 / v[0];
+        case SIN: return std::sin(v[0]);
+        case COS: return std::cos(v[0]);
+        case TAN: return std::tan(v[0]);
+        case ASIN: return std::asin(v[0]);
+        case ACOS: return std::acos(v[0]);
+        case ATAN: return std::atan(v[0]);
+        case EXP: return std::exp(v[0]);
+        case LOG: return std::log(v[0]);
+        case POW: return std::pow(v[0], v[1]);
+        default: return -1.0;
+    }
+}
+
+}  // namespace symgb

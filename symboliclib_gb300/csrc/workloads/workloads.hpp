@@ -1,0 +1,586 @@
+// Synthetic workloads of the engine, written once as model code over a scalar
+// type NT.  Instantiated with the engine's symgb::Symbolic they produce the
+// expressions a ComputeUnit compiles; with double they are the numeric FP64
+// oracle of the same quantity.  The code uses only NT arithmetic (+ - * /,
+// unary -, sqrt found by argument-dependent lookup) and NT(double), so any
+// scalar type with the reference's operator semantics can instantiate it.
+//
+// Sparse assembly sums duplicate triplets left to right in insertion order and
+// stores values column-major with sorted rows (compressed sparse column), the
+// storage order of an Eigen::SparseMatrix built with setFromTriplets.
+#pragma once
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <map>
+#include <utility>
+#include <vector>
+
+namespace symgb_workloads {
+
+// ---------------------------------------------------------------- random
+
+// Seeded generator with a fixed, platform-independent output sequence
+// (splitmix64 seeding of xoshiro256**).
+struct Rng {
+    std::uint64_t s[4];
+    explicit Rng(std::uint64_t seed) {
+        for (auto& w : s) {
+            seed += 0x9e3779b97f4a7c15ULL;
+            std::uint64_t z = seed;
+            z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+            z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+            w = z ^ (z >> 31);
+        }
+    }
+    static std::uint64_t rotl(std::uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+    std::uint64_t next() {
+        const std::uint64_t r = rotl(s[1] * 5, 7) * 9;
+        const std::uint64_t t = s[1] << 17;
+        s[2] ^= s[0];
+        s[3] ^= s[1];
+        s[1] ^= s[2];
+        s[0] ^= s[3];
+        s[2] ^= t;
+        s[3] = rotl(s[3], 45);
+        return r;
+    }
+    double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }  // [0,1)
+    double uniform(double lo, double hi) { return lo + (hi - lo) * uniform(); }
+    std::uint64_t below(std::uint64_t n) { return next() % n; }
+};
+
+// ---------------------------------------------------------------- sparse
+
+template <class NT>
+struct Triplet {
+    int row, col;
+    NT value;
+};
+
+template <class NT>
+struct CSC {
+    int rows = 0, cols = 0;
+    std::vector<int> colPtr, rowIdx;
+    std::vector<NT> values;
+    std::size_t nnz() const { return values.size(); }
+};
+
+// Duplicates are summed as ((t1 + t2) + t3) ... in triplet order.
+template <class NT>
+CSC<NT> assemble(int rows, int cols, const std::vector<Triplet<NT>>& trips) {
+    std::vector<std::map<int, NT>> colsMap(cols);
+    for (const auto& t : trips) {
+        auto& m = colsMap[t.col];
+        auto it = m.find(t.row);
+        if (it == m.end())
+            m.emplace(t.row, t.value);
+        else
+            it->second = it->second + t.value;
+    }
+    CSC<NT> A;
+    A.rows = rows;
+    A.cols = cols;
+    A.colPtr.assign(cols + 1, 0);
+    for (int c = 0; c < cols; ++c) {
+        A.colPtr[c + 1] = A.colPtr[c] + (int)colsMap[c].size();
+        for (auto& e : colsMap[c]) {
+            A.rowIdx.push_back(e.first);
+            A.values.push_back(e.second);
+        }
+    }
+    return A;
+}
+
+// Lower triangle (row >= col) of a CSC matrix.
+template <class NT>
+CSC<NT> lowerTriangle(const CSC<NT>& A) {
+    CSC<NT> L;
+    L.rows = A.rows;
+    L.cols = A.cols;
+    L.colPtr.assign(A.cols + 1, 0);
+    for (int c = 0; c < A.cols; ++c) {
+        for (int k = A.colPtr[c]; k < A.colPtr[c + 1]; ++k)
+            if (A.rowIdx[k] >= c) {
+                L.rowIdx.push_back(A.rowIdx[k]);
+                L.values.push_back(A.values[k]);
+            }
+        L.colPtr[c + 1] = (int)L.values.size();
+    }
+    return L;
+}
+
+// ---------------------------------------------------------------- meshes
+
+struct TriMesh {
+    int nv = 0;
+    std::vector<double> V;  // nv x 3, column-major: V[v + d * nv]
+    std::vector<std::array<int, 3>> F;
+};
+
+// nx x ny vertex grid; every quad split along the (i,j)-(i+1,j+1) diagonal.
+inline std::vector<std::array<int, 3>> gridFaces(int nx, int ny) {
+    std::vector<std::array<int, 3>> F;
+    F.reserve(2 * (nx - 1) * (ny - 1));
+    for (int j = 0; j + 1 < ny; ++j)
+        for (int i = 0; i + 1 < nx; ++i) {
+            const int v00 = i + j * nx, v10 = v00 + 1, v01 = v00 + nx, v11 = v01 + 1;
+            F.push_back({v00, v10, v11});
+            F.push_back({v00, v11, v01});
+        }
+    return F;
+}
+
+// Cotangent-Laplacian mesh: unit-square grid, x,y jittered by +-0.2 spacing,
+// z = 0.1 sin(3x) cos(2y).
+inline TriMesh cotanMesh(int side, std::uint64_t seed) {
+    TriMesh m;
+    m.nv = side * side;
+    m.V.assign(3 * (std::size_t)m.nv, 0.0);
+    const double h = 1.0 / (side - 1);
+    Rng rng(seed);
+    for (int j = 0; j < side; ++j)
+        for (int i = 0; i < side; ++i) {
+            const int v = i + j * side;
+            const double x = i * h + rng.uniform(-0.2 * h, 0.2 * h);
+            const double y = j * h + rng.uniform(-0.2 * h, 0.2 * h);
+            m.V[v] = x;
+            m.V[v + m.nv] = y;
+            m.V[v + 2 * (std::size_t)m.nv] = 0.1 * std::sin(3 * x) * std::cos(2 * y);
+        }
+    m.F = gridFaces(side, side);
+    return m;
+}
+
+// ---------------------------------------------------------------- vector helpers
+
+template <class NT>
+struct Vec3 {
+    NT x, y, z;
+};
+
+template <class NT>
+Vec3<NT> operator-(const Vec3<NT>& a, const Vec3<NT>& b) {
+    return {a.x - b.x, a.y - b.y, a.z - b.z};
+}
+
+template <class NT>
+NT dot(const Vec3<NT>& a, const Vec3<NT>& b) {
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+
+template <class NT>
+Vec3<NT> cross(const Vec3<NT>& a, const Vec3<NT>& b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+template <class NT>
+NT norm(const Vec3<NT>& a) {
+    using std::sqrt;
+    return sqrt(dot(a, a));
+}
+
+template <class NT>
+Vec3<NT> row3(const std::vector<NT>& V, int nv, int v) {
+    return {V[v], V[v + nv], V[v + 2 * (std::size_t)nv]};
+}
+
+// ---------------------------------------------------------------- workload 1: B = A^T A + A
+
+// A: side^2 x side^2; 5-point stencil of a side x side grid plus `extra` random
+// off-diagonal rows per column; pattern only (values are filled by the caller).
+inline CSC<double> stencilMatrix(int side, int extra, std::uint64_t seed) {
+    const int n = side * side;
+    Rng rng(seed);
+    std::vector<Triplet<double>> t;
+    for (int c = 0; c < n; ++c) {
+        const int i = c % side, j = c / side;
+        std::vector<int> rowsC{c};
+        if (i > 0) rowsC.push_back(c - 1);
+        if (i + 1 < side) rowsC.push_back(c + 1);
+        if (j > 0) rowsC.push_back(c - side);
+        if (j + 1 < side) rowsC.push_back(c + side);
+        int added = 0;
+        while (added < extra && n > 6) {
+            const int r = (int)rng.below((std::uint64_t)n);
+            if (std::find(rowsC.begin(), rowsC.end(), r) != rowsC.end()) continue;
+            rowsC.push_back(r);
+            ++added;
+        }
+        for (int r : rowsC) t.push_back({r, c, 1.0});
+    }
+    CSC<double> A = assemble(n, n, t);
+    for (double& v : A.values) v = rng.uniform(-1.0, 1.0);
+    return A;
+}
+
+// Values of A^T A + A on the union pattern.  (A^T A)_ij = sum over k of
+// A_ki A_kj, k ascending; an entry present in both terms is (A^T A)_ij + A_ij.
+template <class NT>
+CSC<NT> ataPlusA(const CSC<double>& pattern, const std::vector<NT>& a) {
+    const int n = pattern.cols;
+    // rows of A: for each row k, the (column, value index) pairs in column order
+    std::vector<std::vector<std::pair<int, int>>> rowsOf(pattern.rows);
+    for (int c = 0; c < n; ++c)
+        for (int k = pattern.colPtr[c]; k < pattern.colPtr[c + 1]; ++k) rowsOf[pattern.rowIdx[k]].push_back({c, k});
+    CSC<NT> B;
+    B.rows = n;
+    B.cols = n;
+    B.colPtr.assign(n + 1, 0);
+    for (int j = 0; j < n; ++j) {
+        std::map<int, NT> acc;
+        for (int kk = pattern.colPtr[j]; kk < pattern.colPtr[j + 1]; ++kk) {
+            const int k = pattern.rowIdx[kk];
+            for (auto& e : rowsOf[k]) {  // A_ki for all columns i of row k
+                NT prod = a[e.second] * a[kk];
+                auto it = acc.find(e.first);
+                if (it == acc.end())
+                    acc.emplace(e.first, prod);
+                else
+                    it->second = it->second + prod;
+            }
+        }
+        for (int kk = pattern.colPtr[j]; kk < pattern.colPtr[j + 1]; ++kk) {
+            const int i = pattern.rowIdx[kk];
+            auto it = acc.find(i);
+            if (it == acc.end())
+                acc.emplace(i, a[kk]);
+            else
+                it->second = it->second + a[kk];
+        }
+        for (auto& e : acc) {
+            B.rowIdx.push_back(e.first);
+            B.values.push_back(e.second);
+        }
+        B.colPtr[j + 1] = (int)B.values.size();
+    }
+    return B;
+}
+
+// ---------------------------------------------------------------- workload 2: cotangent Laplacian
+
+// Per face and corner j with opposite edge (j1, j2): w = dot(e0, e1) / |e0' x e1'|,
+// triplets (j1,j1,-w) (j2,j2,-w) (j1,j2,w) (j2,j1,w).
+template <class NT>
+CSC<NT> cotanLaplacian(const std::vector<NT>& V, int nv, const std::vector<std::array<int, 3>>& F) {
+    std::vector<Triplet<NT>> t;
+    t.reserve(12 * F.size());
+    for (const auto& f : F) {
+        const Vec3<NT> a0 = row3(V, nv, f[0]);
+        const NT area = norm(cross(a0 - row3(V, nv, f[1]), a0 - row3(V, nv, f[2])));
+        for (int j = 0; j < 3; ++j) {
+            const int j1 = f[(j + 1) % 3], j2 = f[(j + 2) % 3];
+            const Vec3<NT> pj = row3(V, nv, f[j]);
+            const NT w = dot(pj - row3(V, nv, j1), pj - row3(V, nv, j2)) / area;
+            t.push_back({j1, j1, -w});
+            t.push_back({j2, j2, -w});
+            t.push_back({j1, j2, w});
+            t.push_back({j2, j1, w});
+        }
+    }
+    return assemble(nv, nv, t);
+}
+
+// ---------------------------------------------------------------- workload 3: Baraff-Witkin cloth
+
+struct ClothParams {
+    double kStretch = 1e3, kStretchDamping = 100.0;
+    double kShear = 1e2, kShearDamping = 1.0;
+    double kBend = 1e-1, kBendDamping = 1e-5;
+    double totalMass = 2.5;
+    double h = 0.05;
+};
+
+// Rest-state quantities (double) of a cloth mesh.
+struct ClothRest {
+    TriMesh mesh;  // rest positions
+    ClothParams p;
+    std::vector<double> area;                 // per face
+    std::vector<std::array<double, 6>> B;     // per face, 3x2 row-major
+    std::vector<std::array<double, 4>> Vinv;  // per face, 2x2 row-major
+    std::vector<std::array<int, 4>> E4;       // interior edges: x0 x1 (edge), x2, x3 (opposite)
+    std::vector<std::array<double, 16>> Q;    // per interior edge, 4x4 bend stiffness
+};
+
+inline double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+inline void cross3(const double* a, const double* b, double* c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+inline double norm3(const double* a) { return std::sqrt(dot3(a, a)); }
+
+// Cloth rest mesh: side x side grid at unit spacing in the plane z = 0.
+inline ClothRest clothRest(int side, const ClothParams& p = ClothParams()) {
+    ClothRest r;
+    r.p = p;
+    TriMesh& m = r.mesh;
+    m.nv = side * side;
+    m.V.assign(3 * (std::size_t)m.nv, 0.0);
+    for (int j = 0; j < side; ++j)
+        for (int i = 0; i < side; ++i) {
+            m.V[i + j * side] = i;
+            m.V[i + j * side + m.nv] = j;
+        }
+    m.F = gridFaces(side, side);
+    auto P = [&](int v, double* o) {
+        for (int d = 0; d < 3; ++d) o[d] = m.V[v + d * (std::size_t)m.nv];
+    };
+    for (const auto& f : m.F) {
+        double p0[3], p1[3], p2[3], v1[3], v2[3], c[3];
+        P(f[0], p0);
+        P(f[1], p1);
+        P(f[2], p2);
+        for (int d = 0; d < 3; ++d) {
+            v1[d] = p1[d] - p0[d];
+            v2[d] = p2[d] - p0[d];
+        }
+        cross3(v1, v2, c);
+        r.area.push_back(0.5 * norm3(c));
+        double u[3], nrm[3], w[3];
+        const double l1 = norm3(v1);
+        for (int d = 0; d < 3; ++d) u[d] = v1[d] / l1;
+        cross3(u, v2, nrm);
+        cross3(nrm, u, w);
+        const double lw = norm3(w);
+        for (int d = 0; d < 3; ++d) w[d] /= lw;
+        const double a = l1, b = dot3(v2, u), c2 = 0.0, d2 = dot3(v2, w);
+        const double det = a * d2 - b * c2;
+        const std::array<double, 4> inv{d2 / det, -b / det, -c2 / det, a / det};
+        r.Vinv.push_back(inv);
+        r.B.push_back({-inv[0] - inv[2], -inv[1] - inv[3], inv[0], inv[1], inv[2], inv[3]});
+    }
+    // Interior edges with the two opposite vertices.
+    std::map<std::pair<int, int>, std::pair<int, int>> edgeFaces;  // (min,max) -> (face, face)
+    for (int fi = 0; fi < (int)m.F.size(); ++fi)
+        for (int e = 0; e < 3; ++e) {
+            const int a = m.F[fi][e], b = m.F[fi][(e + 1) % 3];
+            auto key = std::make_pair(std::min(a, b), std::max(a, b));
+            auto it = edgeFaces.find(key);
+            if (it == edgeFaces.end())
+                edgeFaces.emplace(key, std::make_pair(fi, -1));
+            else
+                it->second.second = fi;
+        }
+    for (auto& ef : edgeFaces) {
+        if (ef.second.second < 0) continue;
+        const auto& f0 = m.F[ef.second.first];
+        const auto& f1 = m.F[ef.second.second];
+        const int x0 = ef.first.first, x1 = ef.first.second;
+        int x2 = -1, x3 = -1;
+        for (int k = 0; k < 3; ++k) {
+            if (f0[k] != x0 && f0[k] != x1) x2 = f0[k];
+            if (f1[k] != x0 && f1[k] != x1) x3 = f1[k];
+        }
+        r.E4.push_back({x0, x1, x2, x3});
+        double x[4][3];
+        for (int k = 0; k < 4; ++k) P(r.E4.back()[k], x[k]);
+        double e0[3], e1[3], e2[3], e3[3], e4[3], ne0[3];
+        for (int d = 0; d < 3; ++d) {
+            e0[d] = x[1][d] - x[0][d];
+            e1[d] = x[2][d] - x[0][d];
+            e2[d] = x[3][d] - x[0][d];
+            e3[d] = x[2][d] - x[1][d];
+            e4[d] = x[3][d] - x[1][d];
+            ne0[d] = -e0[d];
+        }
+        auto cot = [](const double* v, const double* w) {
+            double c[3];
+            cross3(v, w, c);
+            return dot3(v, w) / norm3(c);
+        };
+        const double c01 = cot(e0, e1), c02 = cot(e0, e2), c03 = cot(ne0, e3), c04 = cot(ne0, e4);
+        const double K0[4] = {c03 + c04, c01 + c02, -c01 - c03, -c02 - c04};
+        double c[3];
+        cross3(e0, e1, c);
+        const double A0 = norm3(c);
+        cross3(e0, e2, c);
+        const double A1 = norm3(c);
+        const double coef = -3.0 / (A0 + A1);
+        std::array<double, 16> Q;
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) Q[4 * i + j] = coef * K0[i] * K0[j];
+        r.Q.push_back(Q);
+    }
+    return r;
+}
+
+// Deformed state: rest + sum of three random-phase sinusoids (amplitude 0.05
+// each, per coordinate), velocities uniform in [-0.1, 0.1].
+inline void clothState(const ClothRest& r, std::uint64_t seed, std::vector<double>& X, std::vector<double>& vel) {
+    const int nv = r.mesh.nv;
+    Rng rng(seed);
+    X = r.mesh.V;
+    for (int d = 0; d < 3; ++d)
+        for (int s = 0; s < 3; ++s) {
+            const double kx = rng.uniform(0.05, 0.3), ky = rng.uniform(0.05, 0.3), ph = rng.uniform(0.0, 6.283185307179586);
+            for (int v = 0; v < nv; ++v)
+                X[v + d * (std::size_t)nv] += 0.05 * std::sin(kx * r.mesh.V[v] + ky * r.mesh.V[v + nv] + ph);
+        }
+    vel.resize(3 * (std::size_t)nv);
+    for (auto& v : vel) v = rng.uniform(-0.1, 0.1);
+}
+
+// Lower triangle of A = M - h (D + h K) for the Baraff-Witkin stretch, shear
+// and quadratic bend energies (after the reference example
+// examples/BaraffWitkin: implementation/cloth.cpp:96-110,
+// implementation/stretch_shear_forces_impl.hpp:63-261,
+// implementation/bend_quadratic_forces.cpp:53-155).  `fix(K9, D9)` is applied
+// to every face's 9x9 stiffness and damping blocks (makeFixed for symbolic
+// scalars, nothing for double).
+template <class NT, class Fix>
+CSC<NT> clothMatrix(const ClothRest& r, const std::vector<NT>& X, const std::vector<NT>& Vel, Fix&& fix) {
+    using std::sqrt;
+    const int n = r.mesh.nv;
+    const auto& p = r.p;
+    std::vector<Triplet<NT>> tK, tD;
+    for (std::size_t fi = 0; fi < r.mesh.F.size(); ++fi) {
+        const auto& f = r.mesh.F[fi];
+        const double a = r.area[fi];
+        const auto& Vi = r.Vinv[fi];
+        const auto& B = r.B[fi];
+        auto Bf = [&](int i, int c) { return B[2 * i + c]; };
+        // deformation gradient J = D * Vinv, D = [x1 - x0, x2 - x0]
+        NT Dm[3][2], J[3][2];
+        for (int d = 0; d < 3; ++d) {
+            Dm[d][0] = X[f[1] + d * n] - X[f[0] + d * n];
+            Dm[d][1] = X[f[2] + d * n] - X[f[0] + d * n];
+        }
+        for (int d = 0; d < 3; ++d)
+            for (int c = 0; c < 2; ++c) J[d][c] = Dm[d][0] * NT(Vi[0 + c]) + Dm[d][1] * NT(Vi[2 + c]);
+        NT Jnorm[2], Jn[3][2];
+        for (int c = 0; c < 2; ++c) Jnorm[c] = sqrt(J[0][c] * J[0][c] + J[1][c] * J[1][c] + J[2][c] * J[2][c]);
+        for (int d = 0; d < 3; ++d)
+            for (int c = 0; c < 2; ++c) Jn[d][c] = J[d][c] / Jnorm[c];
+        NT v[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int d = 0; d < 3; ++d) v[i][d] = Vel[f[i] + d * n];
+
+        std::array<NT, 81> K9, D9;
+        // stretch
+        NT C[2] = {NT(a) * (Jnorm[0] - NT(1.0)), NT(a) * (Jnorm[1] - NT(1.0))};
+        NT dC[3][3][2];  // dC[i][d][c]
+        NT Cdot[2] = {NT(0.0), NT(0.0)};
+        for (int i = 0; i < 3; ++i)
+            for (int c = 0; c < 2; ++c) {
+                for (int d = 0; d < 3; ++d) dC[i][d][c] = NT(a * Bf(i, c)) * Jn[d][c];
+                Cdot[c] = Cdot[c] + (dC[i][0][c] * v[i][0] + dC[i][1][c] * v[i][1] + dC[i][2][c] * v[i][2]);
+            }
+        NT IJ[2][3][3];
+        for (int c = 0; c < 2; ++c)
+            for (int d = 0; d < 3; ++d)
+                for (int e = 0; e < 3; ++e)
+                    IJ[c][d][e] = NT(a) * (NT(d == e ? 1.0 : 0.0) - Jn[d][c] * Jn[e][c]) / Jnorm[c];
+        // shear
+        const NT Cs = NT(a) * (J[0][0] * J[0][1] + J[1][0] * J[1][1] + J[2][0] * J[2][1]);
+        NT Cdv[3][3];  // Cdv[i][d]
+        NT Cdots = NT(0.0);
+        for (int i = 0; i < 3; ++i) {
+            for (int d = 0; d < 3; ++d) Cdv[i][d] = NT(a) * (NT(Bf(i, 0)) * J[d][1] + NT(Bf(i, 1)) * J[d][0]);
+            Cdots = Cdots + (Cdv[i][0] * v[i][0] + Cdv[i][1] * v[i][1] + Cdv[i][2] * v[i][2]);
+        }
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                const double bx = Bf(i, 0) * Bf(j, 0), by = Bf(i, 1) * Bf(j, 1);
+                const double dCdvdv = a * (Bf(i, 0) * Bf(j, 1) + Bf(i, 1) * Bf(j, 0));
+                for (int d = 0; d < 3; ++d)
+                    for (int e = 0; e < 3; ++e) {
+                        const NT dxx = NT(bx) * IJ[0][d][e], dyy = NT(by) * IJ[1][d][e];
+                        const NT outer = dC[i][d][0] * dC[j][e][0] + dC[i][d][1] * dC[j][e][1];
+                        NT Ks = NT(-p.kStretch) * (outer + dxx * C[0] + dyy * C[1]);
+                        NT KD = dxx * Cdot[0] + dyy * Cdot[1];
+                        if (d == e) KD = NT(2.0) * KD;
+                        Ks = Ks + NT(-p.kStretchDamping) * KD;
+                        const NT Ds = NT(-p.kStretchDamping) * outer;
+                        const NT so = Cdv[i][d] * Cdv[j][e];
+                        NT Kh = so;
+                        if (d == e) Kh = Kh + NT(dCdvdv) * Cs;
+                        Kh = NT(-p.kShear) * Kh;
+                        if (d == e) Kh = Kh + NT(-p.kShearDamping * dCdvdv) * Cdots;
+                        const NT Dh = NT(-p.kShearDamping) * so;
+                        K9[(3 * i + d) * 9 + 3 * j + e] = Ks + Kh;
+                        D9[(3 * i + d) * 9 + 3 * j + e] = Ds + Dh;
+                    }
+            }
+        fix(K9, D9);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                for (int d = 0; d < 3; ++d)
+                    for (int e = 0; e < 3; ++e) {
+                        const int row = f[i] + d * n, col = f[j] + e * n;
+                        if (row >= col) {
+                            tK.push_back({row, col, K9[(3 * i + d) * 9 + 3 * j + e]});
+                            tD.push_back({row, col, D9[(3 * i + d) * 9 + 3 * j + e]});
+                        }
+                    }
+    }
+    // quadratic bend: constant stiffness k Q and damping kd Q per interior edge
+    std::vector<Triplet<NT>> bK, bD;
+    for (std::size_t e = 0; e < r.E4.size(); ++e)
+        for (int dim = 0; dim < 3; ++dim)
+            for (int v1 = 0; v1 < 4; ++v1)
+                for (int v2 = 0; v2 <= v1; ++v2) {
+                    const int i1 = r.E4[e][v1] + dim * n, i2 = r.E4[e][v2] + dim * n;
+                    const double q = r.Q[e][4 * v1 + v2];
+                    bK.push_back({i1, i2, NT(p.kBend * q)});
+                    bD.push_back({i1, i2, NT(p.kBendDamping * q)});
+                    if (v2 != v1) {
+                        bK.push_back({i2, i1, NT(p.kBend * q)});
+                        bD.push_back({i2, i1, NT(p.kBendDamping * q)});
+                    }
+                }
+    const int N = 3 * n;
+    CSC<NT> Kss = assemble(N, N, tK), Dss = assemble(N, N, tD), Kb = assemble(N, N, bK), Db = assemble(N, N, bD);
+    // A = M - h (D + h K) on the union pattern, lower triangle.
+    const double mass = p.totalMass / n;
+    std::vector<std::map<int, NT>> Kc(N), Dc(N);
+    auto addInto = [](std::vector<std::map<int, NT>>& dst, const CSC<NT>& S) {
+        for (int c = 0; c < S.cols; ++c)
+            for (int k = S.colPtr[c]; k < S.colPtr[c + 1]; ++k) {
+                auto it = dst[c].find(S.rowIdx[k]);
+                if (it == dst[c].end())
+                    dst[c].emplace(S.rowIdx[k], S.values[k]);
+                else
+                    it->second = it->second + S.values[k];
+            }
+    };
+    addInto(Kc, Kss);
+    addInto(Kc, Kb);
+    addInto(Dc, Dss);
+    addInto(Dc, Db);
+    CSC<NT> A;
+    A.rows = N;
+    A.cols = N;
+    A.colPtr.assign(N + 1, 0);
+    for (int c = 0; c < N; ++c) {
+        std::map<int, int> rowsU;
+        for (auto& e : Kc[c]) rowsU[e.first] |= 1;
+        for (auto& e : Dc[c]) rowsU[e.first] |= 2;
+        rowsU[c] |= 4;
+        for (auto& ru : rowsU) {
+            const int row = ru.first;
+            if (row < c) continue;
+            NT inner;
+            if ((ru.second & 3) == 3)
+                inner = Dc[c].at(row) + NT(p.h) * Kc[c].at(row);
+            else if (ru.second & 1)
+                inner = NT(p.h) * Kc[c].at(row);
+            else if (ru.second & 2)
+                inner = Dc[c].at(row);
+            NT val;
+            if (ru.second & 3) {
+                const NT t = NT(p.h) * inner;
+                val = (row == c) ? NT(mass) - t : -t;
+            } else {
+                val = NT(mass);
+            }
+            A.rowIdx.push_back(row);
+            A.values.push_back(val);
+        }
+        A.colPtr[c + 1] = (int)A.values.size();
+    }
+    return A;
+}
+
+}  // namespace symgb_workloads

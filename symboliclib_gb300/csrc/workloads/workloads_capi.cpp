@@ -1,0 +1,146 @@
+// C ABI over the synthetic workloads: builds a workload's expressions with the
+// engine's front end, plans it, and exposes the plan, its tables, the seeded
+// input values and the FP64 values of the same model evaluated in double
+// arithmetic.  Used by the tests and the benchmark through ctypes.
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <sstream>
+#include <string>
+
+#include "symgb/frontend.hpp"
+#include "symgb/plan_image.hpp"
+#include "symgb/utilities.hpp"
+#include "workloads.hpp"
+
+using namespace symgb_workloads;
+
+namespace {
+
+struct Workload {
+    symgb::Plan plan;
+    symgb::PlanImage image;
+    std::vector<std::vector<double>> inputs;
+    std::vector<double> numeric;  // model evaluated in double
+    std::string planText;
+    double frontSeconds = 0.0;
+    std::uint64_t outputs = 0;
+};
+
+thread_local std::string g_err;
+
+std::vector<symgb::Symbolic> variables(std::size_t n, int group) {
+    std::vector<symgb::Symbolic> v;
+    v.reserve(n);
+    for (std::size_t i = 0; i < n; ++i) v.emplace_back((int)i, group);
+    return v;
+}
+
+struct Fix {
+    template <class A>
+    void operator()(A& K9, A& D9) const {
+        symgb::makeFixed(K9, D9);
+    }
+};
+struct NoFix {
+    template <class A>
+    void operator()(A&, A&) const {}
+};
+
+}  // namespace
+
+extern "C" {
+
+typedef struct Workload* symgbw_t;
+
+const char* symgbw_last_error(void) { return g_err.c_str(); }
+
+// workload: "ata" (side), "cotan" (side), "cloth" (side).  vector_width: 0 for
+// the device layout, k > 0 for the reference CPU layout with SIMD width k.
+int symgbw_build(const char* name, int size, unsigned long long seed, int vector_width, int want_text, symgbw_t* out) {
+    try {
+        std::unique_ptr<Workload> w(new Workload());
+        symgb::DeviceConfig dev;
+        dev.vectorWidth = (unsigned)std::max(0, vector_width);
+        dev.cudaDevice = vector_width == 0;
+        symgb::PlanBuilder pb(dev);
+        symgb::Symbolic::uniqueVariableCounter() = 0;
+        const std::string n = name;
+        const auto t0 = std::chrono::steady_clock::now();
+        if (n == "ata") {
+            CSC<double> A = stencilMatrix(size, 2, seed);
+            auto AS = variables(A.nnz(), 0);
+            CSC<symgb::Symbolic> B = ataPlusA(A, AS);
+            pb.addContainer(AS.data(), AS.size());
+            pb.addContainer(B.values.data(), B.values.size());
+            w->inputs.push_back(A.values);
+            w->numeric = ataPlusA(A, A.values).values;
+            w->outputs = B.nnz();
+        } else if (n == "cotan") {
+            TriMesh m = cotanMesh(size, seed);
+            auto VS = variables(m.V.size(), 0);
+            CSC<symgb::Symbolic> L = cotanLaplacian(VS, m.nv, m.F);
+            pb.addContainer(VS.data(), VS.size());
+            pb.addContainer(L.values.data(), L.values.size());
+            w->inputs.push_back(m.V);
+            w->numeric = cotanLaplacian(m.V, m.nv, m.F).values;
+            w->outputs = L.nnz();
+        } else if (n == "cloth") {
+            ClothRest r = clothRest(size);
+            std::vector<double> X, vel;
+            clothState(r, seed, X, vel);
+            auto XS = variables(X.size(), 0), VS = variables(vel.size(), 1);
+            CSC<symgb::Symbolic> A = clothMatrix(r, XS, VS, Fix());
+            pb.addContainer(XS.data(), XS.size());
+            pb.addContainer(VS.data(), VS.size());
+            pb.addContainer(A.values.data(), A.values.size());
+            w->inputs.push_back(X);
+            w->inputs.push_back(vel);
+            w->numeric = clothMatrix(r, X, vel, NoFix()).values;
+            w->outputs = A.nnz();
+        } else {
+            g_err = "unknown workload " + n;
+            return -1;
+        }
+        w->plan = pb.build();
+        w->frontSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        symgb::buildPlanImage(w->plan, w->image, 128);
+        if (want_text) {
+            std::ostringstream os;
+            symgb::dumpPlan(w->plan, os);
+            w->planText = os.str();
+        }
+        *out = w.release();
+        return 0;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+void symgbw_free(symgbw_t w) { delete w; }
+
+const symgb_plan_desc* symgbw_plan(symgbw_t w) { return &w->image.desc; }
+const uint32_t* symgbw_index_data(symgbw_t w) { return w->image.indexData.data(); }
+const uint32_t* symgbw_out_index_data(symgbw_t w) { return w->image.outIndexData.data(); }
+const double* symgbw_const_data(symgbw_t w) { return w->image.constData.data(); }
+int symgbw_num_inputs(symgbw_t w) { return (int)w->inputs.size(); }
+const double* symgbw_input(symgbw_t w, int i, uint64_t* n) {
+    *n = w->inputs[i].size();
+    return w->inputs[i].data();
+}
+const double* symgbw_numeric(symgbw_t w, uint64_t* n) {
+    *n = w->numeric.size();
+    return w->numeric.data();
+}
+uint64_t symgbw_plan_text(symgbw_t w, char* buf, uint64_t cap) {
+    if (buf && cap) {
+        const std::size_t k = std::min<std::size_t>(cap - 1, w->planText.size());
+        std::memcpy(buf, w->planText.data(), k);
+        buf[k] = 0;
+    }
+    return w->planText.size();
+}
+double symgbw_front_seconds(symgbw_t w) { return w->frontSeconds; }
+
+}  // extern "C"

@@ -1,0 +1,253 @@
+"""ctypes bindings of the engine's C ABI (include/symgb.h) and of the workload
+library.  The device path is native code only: if the libraries are missing
+this module raises instead of falling back to anything else."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_DIR = Path(__file__).resolve().parent / "lib"
+
+SCHEDULE_PLAIN, SCHEDULE_LEVELS, SCHEDULE_PERSISTENT = 0, 1, 2
+MATH_EXACT, MATH_FAST = 0, 1
+
+
+class Node(C.Structure):
+    _fields_ = [("op", C.c_int32), ("nchild", C.c_int32), ("a", C.c_int32), ("b", C.c_int32), ("value", C.c_double)]
+
+
+class KernelDesc(C.Structure):
+    _fields_ = [("num_instances", C.c_uint64), ("output_offset", C.c_uint64), ("index_offset", C.c_uint64),
+                ("constants_offset", C.c_uint64), ("num_output_rows", C.c_uint32), ("num_index_rows", C.c_uint32),
+                ("num_constant_rows", C.c_uint32), ("level", C.c_int32), ("num_nodes", C.c_uint32),
+                ("nodes", C.POINTER(Node)), ("num_access", C.c_uint32), ("access", C.POINTER(C.c_int32))]
+
+
+class PlanDesc(C.Structure):
+    _fields_ = [("num_kernels", C.c_uint32), ("kernels", C.POINTER(KernelDesc)), ("num_args", C.c_uint32),
+                ("arg_start", C.POINTER(C.c_uint64)), ("arg_length", C.POINTER(C.c_uint64)),
+                ("num_outputs", C.c_uint32), ("output_start", C.POINTER(C.c_uint64)),
+                ("output_length", C.POINTER(C.c_uint64)), ("num_total_memory", C.c_uint64),
+                ("num_indices", C.c_uint64), ("num_output_values", C.c_uint64), ("num_constants", C.c_uint64),
+                ("threads_per_block", C.c_uint32)]
+
+
+class Schedule(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("math", C.c_int32), ("threads_per_block", C.c_int32),
+                ("items_per_tile", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("num_kernels", "num_levels", "num_inputs", "num_outputs",
+                                           "num_intermediates", "index_entries", "constant_entries", "flops",
+                                           "divs", "sqrts", "transcendentals", "gathers", "max_registers",
+                                           "program_words")]
+
+
+# Every function declared in include/symgb.h, with its ctypes signature.
+SYMGB_FUNCTIONS = {
+    "symgb_unit_create": (C.c_int, [C.POINTER(PlanDesc), C.POINTER(C.c_void_p)]),
+    "symgb_init": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "symgb_set_arg": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "symgb_run": (C.c_int, [C.c_void_p]),
+    "symgb_get_result": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "symgb_finish": (C.c_int, [C.c_void_p]),
+    "symgb_unit_destroy": (None, [C.c_void_p]),
+    "symgb_last_error": (C.c_char_p, []),
+    "symgb_set_schedule": (C.c_int, [C.c_void_p, C.POINTER(Schedule)]),
+    "symgb_get_schedule": (C.c_int, [C.c_void_p, C.POINTER(Schedule)]),
+    "symgb_set_num_sets": (C.c_int, [C.c_void_p, C.c_int]),
+    "symgb_num_sets": (C.c_int, [C.c_void_p]),
+    "symgb_set_arg_sets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "symgb_get_result_sets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "symgb_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "symgb_run_async": (C.c_int, [C.c_void_p]),
+    "symgb_set_arg_sets_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "symgb_get_result_sets_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "symgb_synchronize": (C.c_int, [C.c_void_p]),
+    "symgb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "symgb_algorithmic_bytes": (C.c_uint64, [C.c_void_p, C.c_int]),
+    "symgb_last_launch_count": (C.c_int, [C.c_void_p]),
+}
+
+_libs: dict[str, C.CDLL] = {}
+
+
+def _load(name: str) -> C.CDLL:
+    if name not in _libs:
+        path = LIB_DIR / f"lib{name}.so"
+        if not path.exists():
+            raise RuntimeError(f"{path} is missing: build it with `python -m symboliclib_gb300.build`")
+        _libs[name] = C.CDLL(str(path), mode=C.RTLD_GLOBAL)
+    return _libs[name]
+
+
+def symgb() -> C.CDLL:
+    lib = _load("symgb")
+    if not getattr(lib, "_typed", False):
+        for fn, (res, args) in SYMGB_FUNCTIONS.items():
+            f = getattr(lib, fn)
+            f.restype = res
+            f.argtypes = args
+        lib._typed = True
+    return lib
+
+
+def workloads() -> C.CDLL:
+    symgb()
+    lib = _load("symgb_workloads")
+    if not getattr(lib, "_typed", False):
+        lib.symgbw_build.restype = C.c_int
+        lib.symgbw_build.argtypes = [C.c_char_p, C.c_int, C.c_ulonglong, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+        lib.symgbw_last_error.restype = C.c_char_p
+        lib.symgbw_free.argtypes = [C.c_void_p]
+        lib.symgbw_plan.restype = C.POINTER(PlanDesc)
+        lib.symgbw_plan.argtypes = [C.c_void_p]
+        for fn in ("symgbw_index_data", "symgbw_out_index_data"):
+            getattr(lib, fn).restype = C.POINTER(C.c_uint32)
+            getattr(lib, fn).argtypes = [C.c_void_p]
+        lib.symgbw_const_data.restype = C.POINTER(C.c_double)
+        lib.symgbw_const_data.argtypes = [C.c_void_p]
+        lib.symgbw_num_inputs.argtypes = [C.c_void_p]
+        lib.symgbw_input.restype = C.POINTER(C.c_double)
+        lib.symgbw_input.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_uint64)]
+        lib.symgbw_numeric.restype = C.POINTER(C.c_double)
+        lib.symgbw_numeric.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
+        lib.symgbw_plan_text.restype = C.c_uint64
+        lib.symgbw_plan_text.argtypes = [C.c_void_p, C.c_char_p, C.c_uint64]
+        lib.symgbw_front_seconds.restype = C.c_double
+        lib.symgbw_front_seconds.argtypes = [C.c_void_p]
+        lib._typed = True
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        raise RuntimeError(f"symgb error {rc}: {symgb().symgb_last_error().decode()}")
+
+
+def _array(ptr, n: int, dtype) -> np.ndarray:
+    """Copy of n elements behind a ctypes pointer (empty when n is 0)."""
+    if n == 0:
+        return np.empty(0, dtype)
+    return np.ctypeslib.as_array(ptr, (int(n),)).copy()
+
+
+class Workload:
+    """A synthetic workload planned by the engine's front end."""
+
+    def __init__(self, name: str, size: int, seed: int, vector_width: int = 0, text: bool = False):
+        lib = workloads()
+        h = C.c_void_p()
+        if lib.symgbw_build(name.encode(), size, seed, vector_width, int(text), C.byref(h)) != 0:
+            raise RuntimeError(f"workload {name}: {lib.symgbw_last_error().decode()}")
+        self._lib, self.handle = lib, h
+        self.name, self.size, self.seed = name, size, seed
+        self.plan = lib.symgbw_plan(h)
+        d = self.plan.contents
+        self.num_total_memory = int(d.num_total_memory)
+        self.index_data = _array(lib.symgbw_index_data(h), d.num_indices, np.uint32)
+        self.out_index_data = _array(lib.symgbw_out_index_data(h), d.num_output_values, np.uint32)
+        self.const_data = _array(lib.symgbw_const_data(h), d.num_constants, np.float64)
+        self.inputs = []
+        for i in range(lib.symgbw_num_inputs(h)):
+            n = C.c_uint64()
+            p = lib.symgbw_input(h, i, C.byref(n))
+            self.inputs.append(_array(p, n.value, np.float64))
+        n = C.c_uint64()
+        p = lib.symgbw_numeric(h, C.byref(n))
+        self.numeric = _array(p, n.value, np.float64)
+        self.front_seconds = lib.symgbw_front_seconds(h)
+
+    @property
+    def plan_text(self) -> str:
+        n = self._lib.symgbw_plan_text(self.handle, None, 0)
+        buf = C.create_string_buffer(int(n) + 1)
+        self._lib.symgbw_plan_text(self.handle, buf, n + 1)
+        return buf.value.decode()
+
+    @property
+    def arg_start(self) -> list[int]:
+        d = self.plan.contents
+        return [int(d.arg_start[i]) for i in range(d.num_args)]
+
+    @property
+    def output_length(self) -> list[int]:
+        d = self.plan.contents
+        return [int(d.output_length[i]) for i in range(d.num_outputs)]
+
+    def __del__(self):
+        try:
+            self._lib.symgbw_free(self.handle)
+        except Exception:
+            pass
+
+
+class Unit:
+    """One engine unit (device state for a plan), driven through the C ABI."""
+
+    def __init__(self, plan: C.POINTER(PlanDesc), index_data, out_index_data, const_data):
+        lib = symgb()
+        h = C.c_void_p()
+        check(lib.symgb_unit_create(plan, C.byref(h)))
+        self._lib, self.handle = lib, h
+        self._tables = (np.ascontiguousarray(index_data, np.uint32), np.ascontiguousarray(out_index_data, np.uint32),
+                        np.ascontiguousarray(const_data, np.float64))
+        check(lib.symgb_init(h, *(t.ctypes.data for t in self._tables)))
+        d = plan.contents
+        self.arg_length = [int(d.arg_length[i]) for i in range(d.num_args)]
+        self.output_length = [int(d.output_length[i]) for i in range(d.num_outputs)]
+
+    @classmethod
+    def from_workload(cls, w: Workload) -> "Unit":
+        return cls(w.plan, w.index_data, w.out_index_data, w.const_data)
+
+    def set_schedule(self, kind=SCHEDULE_PLAIN, math=MATH_FAST, threads_per_block=0, items_per_tile=0,
+                     blocks_per_sm=0, use_graph=0) -> None:
+        s = Schedule(kind, math, threads_per_block, items_per_tile, blocks_per_sm, use_graph)
+        check(self._lib.symgb_set_schedule(self.handle, C.byref(s)))
+
+    def set_num_sets(self, n: int) -> None:
+        check(self._lib.symgb_set_num_sets(self.handle, n))
+
+    @property
+    def num_sets(self) -> int:
+        return self._lib.symgb_num_sets(self.handle)
+
+    def set_arg(self, i: int, values: np.ndarray) -> None:
+        v = np.ascontiguousarray(values, np.float64)
+        if v.size != self.arg_length[i] * self.num_sets:
+            raise ValueError("input size mismatch")
+        check(self._lib.symgb_set_arg_sets(self.handle, v.ctypes.data, i))
+
+    def run(self) -> None:
+        check(self._lib.symgb_run(self.handle))
+
+    def get_result(self, k: int = 0) -> np.ndarray:
+        out = np.empty(self.output_length[k] * self.num_sets, np.float64)
+        check(self._lib.symgb_get_result_sets(self.handle, out.ctypes.data, k))
+        return out
+
+    def stats(self) -> Stats:
+        s = Stats()
+        check(self._lib.symgb_get_stats(self.handle, C.byref(s)))
+        return s
+
+    def algorithmic_bytes(self, num_sets: int) -> int:
+        return int(self._lib.symgb_algorithmic_bytes(self.handle, num_sets))
+
+    def last_launch_count(self) -> int:
+        return self._lib.symgb_last_launch_count(self.handle)
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.symgb_unit_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
