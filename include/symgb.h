@@ -104,6 +104,7 @@ typedef struct symgb_schedule {
     int32_t items_per_tile;     /* work items per CTA tile in fused schedules (0 = auto) */
     int32_t blocks_per_sm;      /* persistent grid: CTAs per SM (0 = occupancy maximum) */
     int32_t use_graph;          /* capture run() into a CUDA graph and replay it */
+    int32_t items_per_thread;   /* work items per thread per pass: 1, 2 or 4 (0 = 1) */
 } symgb_schedule;
 
 /* --- the reference's generated-library calls, per unit ----------------------- */
@@ -175,6 +176,16 @@ int symgb_get_stats(symgb_unit_t u, symgb_stats* s);
 /* Algorithmic bytes of one evaluation of `num_sets` value sets:
  * 8 N_in + 8 N_out + 16 N_int per set plus the index and constant tables once. */
 uint64_t symgb_algorithmic_bytes(symgb_unit_t u, int num_sets);
+
+/* Introspection: the device program of kernel k for a math mode (64-bit words
+ * as executed by the interpreter kernels: the load section, then the compute
+ * section).  Writes up to `cap` words, the register count and the length of
+ * the load section; returns the program length in words, or a negative error. */
+int64_t symgb_kernel_program(symgb_unit_t u, int k, int math, uint64_t* words, uint64_t cap, int* registers,
+                             int* num_loads);
+
+/* Measured FP64 FMA throughput of the current device (FLOP/s, one FMA = 2). */
+int symgb_measure_fp64_rate(double* flops_per_second);
 
 /* Number of kernel launches the last run issued (graph replays count the
  * kernels inside the graph). */

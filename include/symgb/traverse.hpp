@@ -19,6 +19,63 @@ struct IdentityHash {
 template <class T>
 using NodeMap = std::unordered_map<long long, T, IdentityHash>;
 
+// Open-addressing map from a 64-bit key (a node identity or hash) to V, for
+// the front end's hot lookup tables.  Only lookup and insert are offered, so
+// unlike an iterated container it cannot change any result order.
+template <class V>
+class KeyMap {
+public:
+    explicit KeyMap(std::size_t expected = 16) {
+        std::size_t cap = 16;
+        while (cap < 2 * expected) cap <<= 1;
+        keys_.assign(cap, kEmpty);
+        vals_.resize(cap);
+    }
+    V& operator[](long long key) {
+        if (2 * (size_ + 1) > keys_.size()) grow();
+        std::size_t i = slot(key);
+        if (keys_[i] == kEmpty) {
+            keys_[i] = key;
+            vals_[i] = V();
+            ++size_;
+        }
+        return vals_[i];
+    }
+    V* find(long long key) {
+        const std::size_t i = slot(key);
+        return keys_[i] == kEmpty ? nullptr : &vals_[i];
+    }
+    std::size_t size() const { return size_; }
+
+private:
+    static constexpr long long kEmpty = (long long)0x8000000000000001ULL;
+    std::size_t slot(long long key) const {
+        const std::size_t mask = keys_.size() - 1;
+        std::size_t i = (std::size_t)(((unsigned long long)key * 0x9e3779b97f4a7c15ULL) >> 17) & mask;
+        while (keys_[i] != kEmpty && keys_[i] != key) i = (i + 1) & mask;
+        return i;
+    }
+    void grow() {
+        std::vector<long long> k;
+        std::vector<V> v;
+        k.swap(keys_);
+        v.swap(vals_);
+        keys_.assign(k.size() * 2, kEmpty);
+        vals_.resize(k.size() * 2);
+        size_ = 0;
+        for (std::size_t j = 0; j < k.size(); ++j)
+            if (k[j] != kEmpty) {
+                const std::size_t i = slot(k[j]);
+                keys_[i] = k[j];
+                vals_[i] = std::move(v[j]);
+                ++size_;
+            }
+    }
+    std::vector<long long> keys_;
+    std::vector<V> vals_;
+    std::size_t size_ = 0;
+};
+
 // Depth-first pre-order with an explicit stack: a node's children are pushed
 // in order and popped last-first (reference Traverse.cpp:11-37).  `fun`
 // returns whether to descend.  With `unique`, each node identity is visited once.

@@ -33,8 +33,8 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 CXX = os.environ.get("CXX", "g++")
 CC = os.environ.get("CC", "gcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-Wno-unused-function", f"-I{INCLUDE}"]
-NVCCFLAGS = ARCH + ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", f"-I{INCLUDE}",
+CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", f"-I{INCLUDE}"]
+NVCCFLAGS = ARCH + ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{INCLUDE}",
                     "-Xptxas", "-warn-spills"]
 
 FRONTEND = sorted((CSRC / "frontend").glob("*.cpp"))

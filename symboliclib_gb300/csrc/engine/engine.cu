@@ -47,12 +47,14 @@ int fail(int code, const std::string& msg) {
 // ------------------------------------------------------------------ device side
 
 struct DevKernel {
-    const std::uint64_t* prog;  // device program
+    const std::uint64_t* prog;  // device program: loads section, then compute words
     const std::uint32_t* p;     // index table of this kernel
     const double* c;            // constant table of this kernel
     std::uint64_t yoff;         // first x slot written by this kernel
     std::uint64_t n;            // instances
     std::uint32_t regs;         // register-file slots used
+    std::uint32_t nloads;       // words in the loads section
+    std::uint32_t nwords;       // total program words (loads + compute)
     std::uint32_t pad;
 };
 
@@ -81,73 +83,6 @@ __device__ __forceinline__ double dfma(double a, double b, double c, int flags) 
     if (flags & symgb::engine::FMA_NEG_PRODUCT) a = -a;
     if (flags & symgb::engine::FMA_NEG_ADDEND) c = -c;
     return __fma_rn(a, b, c);
-}
-
-// Executes one program for one work item.  R points at this thread's first
-// register; registers are `stride` doubles apart (one shared-memory column per
-// thread, so a warp's register access is conflict-free).
-template <int LOAD>
-__device__ __forceinline__ void runProgram(const std::uint64_t* __restrict__ prog, double* R, unsigned stride,
-                                           const double* x, double* xw, const std::uint32_t* __restrict__ p,
-                                           const double* __restrict__ c, std::uint64_t n, std::uint64_t i,
-                                           std::uint64_t yoff, unsigned S, unsigned s) {
-    using namespace symgb::engine;
-#define REG(k) R[(unsigned)(k) * stride]
-    for (const std::uint64_t* ip = prog;;) {
-        const std::uint64_t w = *ip++;
-        const unsigned op = (unsigned)(w & 0xff);
-        const unsigned d = (unsigned)(w >> 8) & 0xff;
-        const unsigned a = (unsigned)(w >> 16) & 0xff;
-        const unsigned b = (unsigned)(w >> 24) & 0xff;
-        switch (op) {
-            case OP_END: return;
-            case OP_LDX: {
-                const unsigned row = (unsigned)(w >> 16) & 0xffff;
-                const int off = (int)(unsigned)(w >> 32);
-                const std::uint64_t slot = (std::uint64_t)((long long)__ldg(p + row * n + i) + off);
-                REG(d) = loadX<LOAD>(x + slot * S + s);
-                break;
-            }
-            case OP_LDC: REG(d) = __ldg(c + (std::uint64_t)(unsigned)(w >> 32) * n + i); break;
-            case OP_LDK: REG(d) = __longlong_as_double((long long)*ip++); break;
-            case OP_ST: xw[(yoff + (std::uint64_t)(unsigned)(w >> 32) * n + i) * S + s] = REG(a); break;
-            case OP_ADD: REG(d) = __dadd_rn(REG(a), REG(b)); break;
-            case OP_SUB: REG(d) = __dsub_rn(REG(a), REG(b)); break;
-            case OP_MUL: REG(d) = __dmul_rn(REG(a), REG(b)); break;
-            case OP_DIV: REG(d) = __ddiv_rn(REG(a), REG(b)); break;
-            case OP_NEG: REG(d) = -REG(a); break;
-            case OP_SQRT: REG(d) = __dsqrt_rn(REG(a)); break;
-            case OP_REC: REG(d) = __ddiv_rn(1.0, REG(a)); break;
-            case OP_FMA: {
-                const unsigned cr = (unsigned)(w >> 32) & 0xff;
-                const int fl = (int)((w >> 40) & 0x3);
-                REG(d) = dfma(REG(a), REG(b), REG(cr), fl);
-                break;
-            }
-            case OP_MOV: REG(d) = REG(a); break;
-            case OP_SIN: REG(d) = sin(REG(a)); break;
-            case OP_COS: REG(d) = cos(REG(a)); break;
-            case OP_TAN: REG(d) = tan(REG(a)); break;
-            case OP_ASIN: REG(d) = asin(REG(a)); break;
-            case OP_ACOS: REG(d) = acos(REG(a)); break;
-            case OP_ATAN: REG(d) = atan(REG(a)); break;
-            case OP_EXP: REG(d) = exp(REG(a)); break;
-            case OP_LOG: REG(d) = log(REG(a)); break;
-            case OP_POW: REG(d) = pow(REG(a), REG(b)); break;
-            default: return;
-        }
-    }
-#undef REG
-}
-
-// One launch per ComputeKernel (the reference's K(i) launch shape).
-__global__ void plainKernel(DevKernel k, const double* x, double* xw, unsigned S) {
-    extern __shared__ double regs[];
-    const std::uint64_t w = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= k.n * S) return;
-    const std::uint64_t i = w / S;
-    const unsigned s = (unsigned)(w - i * S);
-    runProgram<LOAD_CACHED>(k.prog, regs + threadIdx.x, blockDim.x, x, xw, k.p, k.c, k.n, i, k.yoff, S, s);
 }
 
 __device__ __forceinline__ unsigned long long globalTimerNs() {
@@ -191,28 +126,183 @@ __device__ bool gridBarrier(BarrierState* bar, int* hostError, unsigned long lon
     return !failed;
 }
 
-// Tiles of all kernels of levels [levelBegin, levelEnd); levels separated by a
-// grid barrier when the range holds more than one level.
-template <int LOAD>
-__global__ void fusedKernel(const DevKernel* __restrict__ ks, const Tile* __restrict__ tiles,
-                            const std::uint32_t* __restrict__ levelTiles, int levelBegin, int levelEnd,
-                            const double* x, double* xw, unsigned S, BarrierState* bar, int* hostError,
-                            unsigned long long timeoutNs) {
-    extern __shared__ double regs[];
-    for (int L = levelBegin; L < levelEnd; ++L) {
-        const std::uint32_t t0 = levelTiles[L], t1 = levelTiles[L + 1];
-        for (std::uint32_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
-            const Tile tile = tiles[t];
-            const DevKernel k = ks[tile.kernel];
-            for (unsigned j = threadIdx.x; j < tile.count; j += blockDim.x) {
-                const std::uint64_t w = tile.start + j;
-                const std::uint64_t i = w / S;
-                const unsigned s = (unsigned)(w - i * S);
-                runProgram<LOAD>(k.prog, regs + threadIdx.x, blockDim.x, x, xw, k.p, k.c, k.n, i, k.yoff, S, s);
+struct EvalArgs {
+    const DevKernel* ks;
+    const Tile* tiles;
+    const std::uint32_t* segments;  // tile index boundaries of the segments
+    int segBegin, segEnd;           // segments run by this launch, barrier between them
+    const double* x;
+    double* xw;
+    unsigned S;
+    unsigned progCap;               // program words that fit in shared memory (0: read from global)
+    unsigned regStride;             // unused, reserved
+    BarrierState* bar;
+    int* hostError;
+    unsigned long long timeoutNs;
+};
+
+// Evaluates one tile: ITEMS work items per thread.  Shared memory holds the
+// program (when it fits) followed by the register file, laid out
+// [register][item][thread] so a warp's accesses are conflict-free.
+template <int ITEMS, int LOAD>
+__device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t* prog, double* regs, const Tile& t,
+                                         const EvalArgs& A) {
+    using namespace symgb::engine;
+    const unsigned T = blockDim.x;
+    const unsigned S = A.S;
+    for (std::uint64_t base = 0; base < t.count; base += (std::uint64_t)T * ITEMS) {
+        std::uint64_t ii[ITEMS];
+        unsigned ss[ITEMS];
+        bool valid[ITEMS];
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            std::uint64_t off = base + (std::uint64_t)j * T + threadIdx.x;
+            valid[j] = off < t.count;
+            if (!valid[j]) off = t.count - 1;  // duplicate the last item; its stores are skipped
+            const std::uint64_t w = t.start + off;
+            ii[j] = w / S;
+            ss[j] = (unsigned)(w - ii[j] * S);
+        }
+#define REG(r, j) regs[((unsigned)(r) * ITEMS + (j)) * T + threadIdx.x]
+        // Loads: up to 8 entries at a time, all index loads, then all gathers.
+        const unsigned nl = k.nloads;
+        for (unsigned b = 0; b < nl; b += 8) {
+            std::uint64_t wv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) wv[u] = (b + u < nl) ? prog[b + u] : 0ull;
+            long long idx[8][ITEMS];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+#pragma unroll
+                for (int j = 0; j < ITEMS; ++j) {
+                    idx[u][j] = 0;
+                    if ((wv[u] & 0xff) == OP_LDX) {
+                        const unsigned row = (unsigned)(wv[u] >> 16) & 0xffff;
+                        idx[u][j] = (long long)__ldg(k.p + row * k.n + ii[j]) + (int)(unsigned)(wv[u] >> 32);
+                    }
+                }
+            double v[8][ITEMS];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+#pragma unroll
+                for (int j = 0; j < ITEMS; ++j) {
+                    const unsigned op = (unsigned)(wv[u] & 0xff);
+                    if (op == OP_LDX)
+                        v[u][j] = loadX<LOAD>(A.x + (std::uint64_t)idx[u][j] * S + ss[j]);
+                    else if (op == OP_LDC)
+                        v[u][j] = __ldg(k.c + (std::uint64_t)(unsigned)(wv[u] >> 32) * k.n + ii[j]);
+                    else
+                        v[u][j] = 0.0;
+                }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (b + u < nl) {
+                    const unsigned d = (unsigned)(wv[u] >> 8) & 0xff;
+#pragma unroll
+                    for (int j = 0; j < ITEMS; ++j) REG(d, j) = v[u][j];
+                }
+        }
+        // Arithmetic and stores.
+        for (const std::uint64_t* ip = prog + nl;;) {
+            const std::uint64_t w = *ip++;
+            const unsigned op = (unsigned)(w & 0xff);
+            const unsigned d = (unsigned)(w >> 8) & 0xff;
+            const unsigned a = (unsigned)(w >> 16) & 0xff;
+            const unsigned bb = (unsigned)(w >> 24) & 0xff;
+            if (op == OP_END) break;
+            switch (op) {
+                case OP_LDK: {
+                    const double cv = __longlong_as_double((long long)*ip++);
+#pragma unroll
+                    for (int j = 0; j < ITEMS; ++j) REG(d, j) = cv;
+                    break;
+                }
+                case OP_ST: {
+                    const std::uint64_t row = (std::uint64_t)(unsigned)(w >> 32);
+#pragma unroll
+                    for (int j = 0; j < ITEMS; ++j)
+                        if (valid[j]) A.xw[(k.yoff + row * k.n + ii[j]) * S + ss[j]] = REG(a, j);
+                    break;
+                }
+#define BIN(OPC, EXPR)                                                 \
+    case OPC: {                                                        \
+        _Pragma("unroll") for (int j = 0; j < ITEMS; ++j) {            \
+            const double x1 = REG(a, j), x2 = REG(bb, j);              \
+            REG(d, j) = (EXPR);                                        \
+        }                                                              \
+        break;                                                         \
+    }
+#define UN(OPC, EXPR)                                                  \
+    case OPC: {                                                        \
+        _Pragma("unroll") for (int j = 0; j < ITEMS; ++j) {            \
+            const double x1 = REG(a, j);                               \
+            REG(d, j) = (EXPR);                                        \
+        }                                                              \
+        break;                                                         \
+    }
+                BIN(OP_ADD, __dadd_rn(x1, x2))
+                BIN(OP_SUB, __dsub_rn(x1, x2))
+                BIN(OP_MUL, __dmul_rn(x1, x2))
+                BIN(OP_DIV, __ddiv_rn(x1, x2))
+                BIN(OP_POW, pow(x1, x2))
+                UN(OP_NEG, -x1)
+                UN(OP_SQRT, __dsqrt_rn(x1))
+                UN(OP_REC, __ddiv_rn(1.0, x1))
+                UN(OP_MOV, x1)
+                UN(OP_SIN, sin(x1))
+                UN(OP_COS, cos(x1))
+                UN(OP_TAN, tan(x1))
+                UN(OP_ASIN, asin(x1))
+                UN(OP_ACOS, acos(x1))
+                UN(OP_ATAN, atan(x1))
+                UN(OP_EXP, exp(x1))
+                UN(OP_LOG, log(x1))
+#undef BIN
+#undef UN
+                case OP_FMA: {
+                    const unsigned cr = (unsigned)(w >> 32) & 0xff;
+                    const int fl = (int)((w >> 40) & 0x3);
+#pragma unroll
+                    for (int j = 0; j < ITEMS; ++j) REG(d, j) = dfma(REG(a, j), REG(bb, j), REG(cr, j), fl);
+                    break;
+                }
+                default: break;
             }
         }
-        if (L + 1 < levelEnd)
-            if (!gridBarrier(bar, hostError, timeoutNs)) return;
+#undef REG
+    }
+}
+
+// Runs the tiles of segments [segBegin, segEnd); a grid barrier separates
+// segments (cooperative launches only when the range holds several segments).
+template <int ITEMS, int LOAD>
+__global__ void evalKernel(EvalArgs A) {
+    extern __shared__ double smem[];
+    std::uint64_t* progSmem = reinterpret_cast<std::uint64_t*>(smem);
+    double* regs = smem + A.progCap;
+    int cur = -1;
+    const std::uint64_t* prog = nullptr;
+    DevKernel k;
+    for (int sg = A.segBegin; sg < A.segEnd; ++sg) {
+        const std::uint32_t t0 = A.segments[sg], t1 = A.segments[sg + 1];
+        for (std::uint32_t ti = t0 + blockIdx.x; ti < t1; ti += gridDim.x) {
+            const Tile t = A.tiles[ti];
+            if ((int)t.kernel != cur) {
+                k = A.ks[t.kernel];
+                cur = (int)t.kernel;
+                if (k.nwords <= A.progCap) {
+                    __syncthreads();  // previous program no longer in use
+                    for (unsigned q = threadIdx.x; q < k.nwords; q += blockDim.x) progSmem[q] = k.prog[q];
+                    __syncthreads();
+                    prog = progSmem;
+                } else {
+                    prog = k.prog;
+                }
+            }
+            evalTile<ITEMS, LOAD>(k, prog, regs, t, A);
+        }
+        if (sg + 1 < A.segEnd)
+            if (!gridBarrier(A.bar, A.hostError, A.timeoutNs)) return;
     }
 }
 
@@ -273,27 +363,28 @@ struct symgb_unit {
     std::uint64_t numTotalMemory = 0, numIndices = 0, numOutputValues = 0, numConstants = 0;
     int threadsPerBlock = 128;
     int numLevels = 0;
-    symgb_schedule sched{SYMGB_SCHEDULE_PLAIN, SYMGB_MATH_FAST, 0, 0, 0, 0};
+    symgb_schedule sched{SYMGB_SCHEDULE_PLAIN, SYMGB_MATH_FAST, 0, 0, 0, 0, 1};
     int numSets = 1;
 
     // device state
     bool initialized = false;
     int device = 0;
     int smCount = 0;
+    std::size_t smemOptin = 48 * 1024;  // max dynamic shared memory per block
     cudaStream_t ownStream = nullptr, stream = nullptr;
     DevBuf<double> x, c, staging, outBuf;
     DevBuf<std::uint32_t> p, ids;
     DevBuf<std::uint64_t> progs;
     DevBuf<DevKernel> devKernels;
     DevBuf<Tile> tiles;
-    DevBuf<std::uint32_t> levelTiles;
+    DevBuf<std::uint32_t> levelSeg, kernelSeg;
     DevBuf<BarrierState> barrier;
     int* errorHost = nullptr;  // mapped pinned flag written by the device
     int* errorDev = nullptr;
     std::vector<DevKernel> hostDevKernels;
-    std::vector<std::uint32_t> hostLevelTiles;
+    std::vector<std::uint32_t> hostLevelSeg, hostKernelSeg;  // tile boundaries per level / per kernel
     std::vector<Tile> hostTiles;
-    std::vector<int> kernelOrderByLevel;
+    std::uint32_t maxProgWords = 0;
     std::size_t tilesFor = 0;  // configuration the tile table was built for
     int tilesSets = -1, tilesItems = -1, tilesMath = -1;
     cudaGraphExec_t graph = nullptr;
@@ -321,7 +412,8 @@ struct symgb_unit {
         progs.reset();
         devKernels.reset();
         tiles.reset();
-        levelTiles.reset();
+        levelSeg.reset();
+        kernelSeg.reset();
         barrier.reset();
         if (errorHost) cudaFreeHost(errorHost);
         errorHost = nullptr;
@@ -334,6 +426,7 @@ struct symgb_unit {
 
     int mathIndex() const { return sched.math == SYMGB_MATH_EXACT ? 0 : 1; }
     int tpb() const { return sched.threads_per_block > 0 ? sched.threads_per_block : threadsPerBlock; }
+    int items() const { return sched.items_per_thread == 2 || sched.items_per_thread == 4 ? sched.items_per_thread : 1; }
 };
 
 namespace {
@@ -342,22 +435,29 @@ int uploadPrograms(symgb_unit* u) {
     const int mi = u->mathIndex();
     std::vector<std::uint64_t> all;
     std::vector<std::size_t> offs;
+    u->maxProgWords = 0;
     for (auto& k : u->kernels) {
         offs.push_back(all.size());
-        all.insert(all.end(), k.prog[mi].words.begin(), k.prog[mi].words.end());
+        const Program& pr = k.prog[mi];
+        all.insert(all.end(), pr.loads.begin(), pr.loads.end());
+        all.insert(all.end(), pr.words.begin(), pr.words.end());
+        u->maxProgWords = std::max<std::uint32_t>(u->maxProgWords, (std::uint32_t)(pr.loads.size() + pr.words.size()));
     }
     SYMGB_CUDA(u->progs.alloc(all.size()));
     SYMGB_CUDA(cudaMemcpy(u->progs.ptr, all.data(), all.size() * 8, cudaMemcpyHostToDevice));
     u->hostDevKernels.clear();
     for (std::size_t k = 0; k < u->kernels.size(); ++k) {
         const auto& d = u->kernels[k].desc;
+        const Program& pr = u->kernels[k].prog[mi];
         DevKernel dk;
         dk.prog = u->progs.ptr + offs[k];
         dk.p = u->p.ptr + d.index_offset;
         dk.c = u->c.ptr + d.constants_offset;
         dk.yoff = d.output_offset;
         dk.n = d.num_instances;
-        dk.regs = (std::uint32_t)std::max(1, u->kernels[k].prog[mi].registers);
+        dk.regs = (std::uint32_t)std::max(1, pr.registers);
+        dk.nloads = (std::uint32_t)pr.loads.size();
+        dk.nwords = (std::uint32_t)(pr.loads.size() + pr.words.size());
         dk.pad = 0;
         u->hostDevKernels.push_back(dk);
     }
@@ -369,39 +469,62 @@ int uploadPrograms(symgb_unit* u) {
     return SYMGB_OK;
 }
 
-// Tile table for the fused schedules: per level, every kernel's work items cut
-// into tiles of `items` consecutive work items.
+// Tile table: per level, every kernel's work items cut into tiles of
+// consecutive work items; tiles of one kernel are contiguous.  Segments give the
+// tile boundaries per level (fused schedules) and per kernel (plain schedule).
 int buildTiles(symgb_unit* u) {
     const int S = u->numSets;
-    int items = u->sched.items_per_tile > 0 ? u->sched.items_per_tile : 2 * u->tpb();
+    const int items = u->sched.items_per_tile > 0 ? u->sched.items_per_tile : u->tpb() * u->items();
     if (u->tilesSets == S && u->tilesItems == items && u->tilesMath == u->mathIndex()) return SYMGB_OK;
     u->hostTiles.clear();
-    u->hostLevelTiles.assign(1, 0);
+    u->hostLevelSeg.assign(1, 0);
+    u->hostKernelSeg.assign(1, 0);
     for (int L = 0; L < u->numLevels; ++L) {
         for (std::size_t k = 0; k < u->kernels.size(); ++k) {
             if (u->kernels[k].desc.level != L) continue;
             const std::uint64_t total = u->kernels[k].desc.num_instances * (std::uint64_t)S;
+            if (!total) continue;
             for (std::uint64_t st = 0; st < total; st += items)
                 u->hostTiles.push_back({(std::uint32_t)k, (std::uint32_t)std::min<std::uint64_t>(items, total - st), st});
+            u->hostKernelSeg.push_back((std::uint32_t)u->hostTiles.size());
         }
-        u->hostLevelTiles.push_back((std::uint32_t)u->hostTiles.size());
+        u->hostLevelSeg.push_back((std::uint32_t)u->hostTiles.size());
     }
     SYMGB_CUDA(u->tiles.alloc(u->hostTiles.size()));
     if (!u->hostTiles.empty())
         SYMGB_CUDA(cudaMemcpy(u->tiles.ptr, u->hostTiles.data(), u->hostTiles.size() * sizeof(Tile), cudaMemcpyHostToDevice));
-    SYMGB_CUDA(u->levelTiles.alloc(u->hostLevelTiles.size()));
-    SYMGB_CUDA(cudaMemcpy(u->levelTiles.ptr, u->hostLevelTiles.data(), u->hostLevelTiles.size() * 4, cudaMemcpyHostToDevice));
+    SYMGB_CUDA(u->levelSeg.alloc(u->hostLevelSeg.size()));
+    SYMGB_CUDA(cudaMemcpy(u->levelSeg.ptr, u->hostLevelSeg.data(), u->hostLevelSeg.size() * 4, cudaMemcpyHostToDevice));
+    SYMGB_CUDA(u->kernelSeg.alloc(u->hostKernelSeg.size()));
+    SYMGB_CUDA(cudaMemcpy(u->kernelSeg.ptr, u->hostKernelSeg.data(), u->hostKernelSeg.size() * 4, cudaMemcpyHostToDevice));
     u->tilesSets = S;
     u->tilesItems = items;
     u->tilesMath = u->mathIndex();
     return SYMGB_OK;
 }
 
-std::size_t regBytes(const symgb_unit* u, int kbegin, int kend, int tpb, int level = -1) {
+std::uint32_t maxRegs(const symgb_unit* u, int level = -1) {
     std::uint32_t r = 1;
-    for (int k = kbegin; k < kend; ++k)
+    for (std::size_t k = 0; k < u->kernels.size(); ++k)
         if (level < 0 || u->kernels[k].desc.level == level) r = std::max(r, u->hostDevKernels[k].regs);
-    return (std::size_t)r * tpb * sizeof(double);
+    return r;
+}
+
+// Program words kept in shared memory per CTA (larger programs are read from
+// global memory through the L1 cache).
+constexpr std::uint32_t kProgCapWords = 4096;
+
+std::uint32_t progCap(const symgb_unit* u) { return std::min(u->maxProgWords, kProgCapWords); }
+
+std::size_t smemBytes(const symgb_unit* u, std::uint32_t regs, int items, int tpb) {
+    return (std::size_t)progCap(u) * 8 + (std::size_t)regs * items * tpb * sizeof(double);
+}
+
+// Largest block size <= tpb (a multiple of 32) whose program and register file
+// fit in shared memory; 0 if not even one warp fits.
+int fitBlock(const symgb_unit* u, std::uint32_t regs, int items, int tpb) {
+    while (tpb >= 32 && smemBytes(u, regs, items, tpb) > u->smemOptin) tpb -= 32;
+    return tpb >= 32 ? tpb : 0;
 }
 
 int setSmemLimit(const void* fn, std::size_t bytes) {
@@ -409,66 +532,83 @@ int setSmemLimit(const void* fn, std::size_t bytes) {
     return SYMGB_OK;
 }
 
+const void* evalFunction(int items, bool l2) {
+    switch (items) {
+        case 2: return l2 ? (const void*)evalKernel<2, LOAD_L2> : (const void*)evalKernel<2, LOAD_CACHED>;
+        case 4: return l2 ? (const void*)evalKernel<4, LOAD_L2> : (const void*)evalKernel<4, LOAD_CACHED>;
+        default: return l2 ? (const void*)evalKernel<1, LOAD_L2> : (const void*)evalKernel<1, LOAD_CACHED>;
+    }
+}
+
 // Enqueues one evaluation on the unit's stream.
 int enqueueRun(symgb_unit* u) {
-    const unsigned S = (unsigned)u->numSets;
+    if (int e = buildTiles(u)) return e;
+    const int items = u->items();
     const int tpb = u->tpb();
     int launches = 0;
+    EvalArgs A;
+    A.ks = u->devKernels.ptr;
+    A.tiles = u->tiles.ptr;
+    A.x = u->x.ptr;
+    A.xw = u->x.ptr;
+    A.S = (unsigned)u->numSets;
+    A.progCap = progCap(u);
+    A.regStride = 0;
+    A.bar = u->barrier.ptr;
+    A.hostError = u->errorDev;
+    A.timeoutNs = u->barrierTimeoutNs;
+    auto launch = [&](bool l2, std::uint32_t regs, unsigned grid, bool coop) -> int {
+        const int bt = fitBlock(u, regs, items, tpb);
+        if (!bt) return fail(SYMGB_ERR_ARGUMENT, "kernel register file exceeds shared memory");
+        const std::size_t smem = smemBytes(u, regs, items, bt);
+        const void* fn = evalFunction(items, l2);
+        if (setSmemLimit(fn, smem)) return SYMGB_ERR_CUDA;
+        if (coop) {
+            int perSm = 0;
+            SYMGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fn, bt, smem));
+            if (perSm < 1) return fail(SYMGB_ERR_ARGUMENT, "persistent schedule: register file does not fit on an SM");
+            if (u->sched.blocks_per_sm > 0) perSm = std::min(perSm, u->sched.blocks_per_sm);
+            grid = std::max(1u, std::min<unsigned>(grid, (unsigned)(perSm * u->smCount)));
+            void* args[] = {(void*)&A};
+            SYMGB_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(bt), args, smem, u->stream));
+        } else {
+            void* args[] = {(void*)&A};
+            SYMGB_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(bt), args, smem, u->stream));
+        }
+        ++launches;
+        return SYMGB_OK;
+    };
     switch (u->sched.kind) {
         case SYMGB_SCHEDULE_PLAIN: {
-            for (std::size_t k = 0; k < u->kernels.size(); ++k) {
-                const DevKernel& dk = u->hostDevKernels[k];
-                const std::uint64_t work = dk.n * S;
-                if (work == 0) continue;
-                const std::size_t smem = (std::size_t)dk.regs * tpb * sizeof(double);
-                if (setSmemLimit((const void*)plainKernel, smem)) return SYMGB_ERR_CUDA;
-                const unsigned grid = (unsigned)((work + tpb - 1) / tpb);
-                plainKernel<<<grid, tpb, smem, u->stream>>>(dk, u->x.ptr, u->x.ptr, S);
-                ++launches;
+            A.segments = u->kernelSeg.ptr;
+            for (std::size_t sgi = 0; sgi + 1 < u->hostKernelSeg.size(); ++sgi) {
+                const std::uint32_t nt = u->hostKernelSeg[sgi + 1] - u->hostKernelSeg[sgi];
+                const std::uint32_t k = u->hostTiles[u->hostKernelSeg[sgi]].kernel;
+                A.segBegin = (int)sgi;
+                A.segEnd = (int)sgi + 1;
+                if (int e = launch(false, u->hostDevKernels[k].regs, nt, false)) return e;
             }
             break;
         }
         case SYMGB_SCHEDULE_LEVELS: {
-            if (int e = buildTiles(u)) return e;
+            A.segments = u->levelSeg.ptr;
             for (int L = 0; L < u->numLevels; ++L) {
-                const std::uint32_t nt = u->hostLevelTiles[L + 1] - u->hostLevelTiles[L];
+                const std::uint32_t nt = u->hostLevelSeg[L + 1] - u->hostLevelSeg[L];
                 if (!nt) continue;
-                const std::size_t smem = regBytes(u, 0, (int)u->kernels.size(), tpb, L);
-                if (setSmemLimit((const void*)fusedKernel<LOAD_CACHED>, smem)) return SYMGB_ERR_CUDA;
-                fusedKernel<LOAD_CACHED><<<nt, tpb, smem, u->stream>>>(u->devKernels.ptr, u->tiles.ptr, u->levelTiles.ptr, L,
-                                                                      L + 1, u->x.ptr, u->x.ptr, S, u->barrier.ptr,
-                                                                      u->errorDev, u->barrierTimeoutNs);
-                ++launches;
+                A.segBegin = L;
+                A.segEnd = L + 1;
+                if (int e = launch(false, maxRegs(u, L), nt, false)) return e;
             }
             break;
         }
         case SYMGB_SCHEDULE_PERSISTENT: {
-            if (int e = buildTiles(u)) return e;
-            const std::size_t smem = regBytes(u, 0, (int)u->kernels.size(), tpb);
-            const void* fn = (const void*)fusedKernel<LOAD_L2>;
-            if (setSmemLimit(fn, smem)) return SYMGB_ERR_CUDA;
-            int perSm = 0;
-            SYMGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fusedKernel<LOAD_L2>, tpb, smem));
-            if (perSm < 1) return fail(SYMGB_ERR_ARGUMENT, "persistent schedule: register file does not fit on an SM");
-            if (u->sched.blocks_per_sm > 0) perSm = std::min(perSm, u->sched.blocks_per_sm);
-            unsigned grid = (unsigned)(perSm * u->smCount);
-            std::uint32_t maxTiles = 0;
+            A.segments = u->levelSeg.ptr;
+            A.segBegin = 0;
+            A.segEnd = u->numLevels;
+            std::uint32_t maxTiles = 1;
             for (int L = 0; L < u->numLevels; ++L)
-                maxTiles = std::max(maxTiles, u->hostLevelTiles[L + 1] - u->hostLevelTiles[L]);
-            grid = std::max(1u, std::min<unsigned>(grid, maxTiles));
-            const DevKernel* ks = u->devKernels.ptr;
-            const Tile* tl = u->tiles.ptr;
-            const std::uint32_t* lt = u->levelTiles.ptr;
-            int lb = 0, le = u->numLevels;
-            const double* xr = u->x.ptr;
-            double* xw = u->x.ptr;
-            BarrierState* bar = u->barrier.ptr;
-            int* err = u->errorDev;
-            unsigned long long to = u->barrierTimeoutNs;
-            void* args[] = {(void*)&ks, (void*)&tl, (void*)&lt, (void*)&lb, (void*)&le, (void*)&xr,
-                            (void*)&xw, (void*)&S, (void*)&bar, (void*)&err, (void*)&to};
-            SYMGB_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(tpb), args, smem, u->stream));
-            ++launches;
+                maxTiles = std::max(maxTiles, u->hostLevelSeg[L + 1] - u->hostLevelSeg[L]);
+            if (int e = launch(true, maxRegs(u), maxTiles, true)) return e;
             break;
         }
         default: return fail(SYMGB_ERR_ARGUMENT, "unknown schedule kind");
@@ -482,8 +622,7 @@ int runAsync(symgb_unit* u) {
     if (!u->initialized) return fail(SYMGB_ERR_STATE, "run before init");
     if (u->sched.use_graph && u->sched.kind != SYMGB_SCHEDULE_PERSISTENT) {
         if (!u->graphValid) {
-            if (u->sched.kind != SYMGB_SCHEDULE_PLAIN)
-                if (int e = buildTiles(u)) return e;
+            if (int e = buildTiles(u)) return e;
             // smem attributes must be set outside capture
             cudaGraph_t g;
             SYMGB_CUDA(cudaStreamBeginCapture(u->stream, cudaStreamCaptureModeThreadLocal));
@@ -597,6 +736,9 @@ int symgb_init(symgb_unit_t u, const uint32_t* index_data, const uint32_t* out_i
     u->release();
     SYMGB_CUDA(cudaGetDevice(&u->device));
     SYMGB_CUDA(cudaDeviceGetAttribute(&u->smCount, cudaDevAttrMultiProcessorCount, u->device));
+    int optin = 0;
+    SYMGB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, u->device));
+    u->smemOptin = (std::size_t)optin;
     SYMGB_CUDA(cudaStreamCreateWithFlags(&u->ownStream, cudaStreamNonBlocking));
     u->stream = u->ownStream;
     SYMGB_CUDA(u->x.alloc(u->numTotalMemory * (std::size_t)u->numSets));
@@ -724,6 +866,9 @@ void symgb_unit_destroy(symgb_unit_t u) {
 int symgb_set_schedule(symgb_unit_t u, const symgb_schedule* s) {
     if (!u || !s) return fail(SYMGB_ERR_ARGUMENT, "null argument");
     if (s->kind < 0 || s->kind > 2 || s->math < 0 || s->math > 1) return fail(SYMGB_ERR_ARGUMENT, "bad schedule");
+    if (s->items_per_thread != 0 && s->items_per_thread != 1 && s->items_per_thread != 2 && s->items_per_thread != 4)
+        return fail(SYMGB_ERR_ARGUMENT, "items_per_thread must be 1, 2 or 4");
+    if (s->items_per_tile < 0 || s->blocks_per_sm < 0) return fail(SYMGB_ERR_ARGUMENT, "negative schedule parameter");
     if (s->threads_per_block < 0 || s->threads_per_block > 1024 || (s->threads_per_block % 32))
         return fail(SYMGB_ERR_ARGUMENT, "threads_per_block must be a multiple of 32 up to 1024");
     const bool mathChanged = s->math != u->sched.math;
@@ -799,5 +944,18 @@ uint64_t symgb_algorithmic_bytes(symgb_unit_t u, int num_sets) {
 }
 
 int symgb_last_launch_count(symgb_unit_t u) { return u ? u->lastLaunches : 0; }
+
+int64_t symgb_kernel_program(symgb_unit_t u, int k, int math, uint64_t* words, uint64_t cap, int* registers,
+                             int* num_loads) {
+    if (!u || k < 0 || (std::size_t)k >= u->kernels.size() || math < 0 || math > 1)
+        return fail(SYMGB_ERR_ARGUMENT, "bad kernel or math mode");
+    const Program& pr = u->kernels[k].prog[math];
+    std::vector<std::uint64_t> all(pr.loads);
+    all.insert(all.end(), pr.words.begin(), pr.words.end());
+    if (words) std::memcpy(words, all.data(), std::min<std::uint64_t>(cap, all.size()) * sizeof(std::uint64_t));
+    if (registers) *registers = pr.registers;
+    if (num_loads) *num_loads = (int)pr.loads.size();
+    return (int64_t)all.size();
+}
 
 }  // extern "C"

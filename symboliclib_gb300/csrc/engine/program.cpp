@@ -41,9 +41,26 @@ public:
         if (stack.size() != 1) throw std::runtime_error("template is not a single tree");
         root_ = stack.back();
         countLocalUses(root_);
+        collectLoads(root_);
     }
 
     Program run() {
+        // Load section: one register per distinct load, in first-use order.
+        for (auto& key : loadOrder_) {
+            const int d = alloc();
+            loadReg_[key] = d;
+            const int kind = (int)(key >> 62);
+            if (kind == 1) {  // gather
+                const int row = (int)((key >> 32) & 0xffff);
+                const std::int32_t off = (std::int32_t)(std::uint32_t)(key & 0xffffffffu);
+                prog_.loads.push_back((std::uint64_t)OP_LDX | ((std::uint64_t)d << 8) | ((std::uint64_t)row << 16) |
+                                      ((std::uint64_t)(std::uint32_t)off << 32));
+                ++prog_.stats.gathers;
+            } else {  // per-instance constant
+                const std::uint32_t row = (std::uint32_t)(key & 0xffffffffu);
+                prog_.loads.push_back(encode(OP_LDC, d, 0, 0, row));
+            }
+        }
         const symgb_node& r = k_.nodes[root_];
         if (r.op == N_BLOCK) {
             for (int s : kids_[root_]) statement(s);
@@ -57,6 +74,28 @@ public:
 
 private:
     const symgb_node& node(int j) const { return k_.nodes[j]; }
+
+    // Key of a load leaf: kind (1 gather, 2 constant) in bits 62-63.
+    std::uint64_t loadKey(const symgb_node& nd) const {
+        if (nd.b == G_INDEX) {
+            if (nd.a < 0 || (std::uint32_t)nd.a >= k_.num_access) throw std::runtime_error("index variable out of range");
+            const int row = k_.access[2 * nd.a], off = k_.access[2 * nd.a + 1];
+            if (row < 0 || row > 0xffff || (std::uint32_t)row >= k_.num_index_rows)
+                throw std::runtime_error("index row out of range");
+            return (1ull << 62) | ((std::uint64_t)row << 32) | (std::uint64_t)(std::uint32_t)off;
+        }
+        if (nd.a < 0 || (std::uint32_t)nd.a >= k_.num_constant_rows) throw std::runtime_error("constant row out of range");
+        return (2ull << 62) | (std::uint64_t)(std::uint32_t)nd.a;
+    }
+
+    void collectLoads(int j) {
+        const symgb_node& nd = node(j);
+        if (nd.op == N_VAR && (nd.b == G_INDEX || nd.b == G_CONSTANT)) {
+            const std::uint64_t key = loadKey(nd);
+            if (loadUses_[key]++ == 0) loadOrder_.push_back(key);
+        }
+        for (int c : kids_[j]) collectLoads(c);
+    }
 
     void countLocalUses(int j) {
         const symgb_node& nd = node(j);
@@ -210,22 +249,12 @@ private:
                     const bool last = --uses_[nd.a] == 0;
                     return {it->second, last};
                 }
-                const int d = alloc();
-                if (nd.b == G_INDEX) {
-                    if (nd.a < 0 || (std::uint32_t)nd.a >= k_.num_access) throw std::runtime_error("index variable out of range");
-                    const int row = k_.access[2 * nd.a], off = k_.access[2 * nd.a + 1];
-                    if (row < 0 || row > 0xffff || (std::uint32_t)row >= k_.num_index_rows)
-                        throw std::runtime_error("index row out of range");
-                    emit((std::uint64_t)OP_LDX | ((std::uint64_t)d << 8) | ((std::uint64_t)row << 16) |
-                         ((std::uint64_t)(std::uint32_t)off << 32));
-                    ++prog_.stats.gathers;
-                } else if (nd.b == G_CONSTANT) {
-                    if (nd.a < 0 || (std::uint32_t)nd.a >= k_.num_constant_rows) throw std::runtime_error("constant row out of range");
-                    emit(encode(OP_LDC, d, 0, 0, (std::uint32_t)nd.a));
-                } else {
-                    throw std::runtime_error("unsupported variable group in template");
+                if (nd.b == G_INDEX || nd.b == G_CONSTANT) {
+                    const std::uint64_t key = loadKey(nd);
+                    const bool last = --loadUses_[key] == 0;
+                    return {loadReg_.at(key), last};
                 }
-                return {d, true};
+                throw std::runtime_error("unsupported variable group in template");
             }
             case N_ADD: return sum(j);
             case N_MUL: return product(j);
@@ -310,6 +339,8 @@ private:
     std::vector<std::vector<int>> kids_;
     int root_ = 0;
     std::unordered_map<int, int> uses_, regOf_;
+    std::unordered_map<std::uint64_t, int> loadUses_, loadReg_;
+    std::vector<std::uint64_t> loadOrder_;
     std::vector<int> free_;
     int maxReg_ = 0;
     Program prog_;
@@ -327,8 +358,10 @@ std::string disassemble(const Program& p) {
                                              "rec", "fma", "sin", "cos", "tan", "asin", "acos", "atan", "exp", "log",
                                              "pow", "mov"};
     std::ostringstream os;
-    for (std::size_t pc = 0; pc < p.words.size(); ++pc) {
-        const std::uint64_t w = p.words[pc];
+    std::vector<std::uint64_t> all(p.loads);
+    all.insert(all.end(), p.words.begin(), p.words.end());
+    for (std::size_t pc = 0; pc < all.size(); ++pc) {
+        const std::uint64_t w = all[pc];
         const int op = (int)(w & 0xff), d = (int)((w >> 8) & 0xff), a = (int)((w >> 16) & 0xff),
                   b = (int)((w >> 24) & 0xff);
         const std::int32_t imm = (std::int32_t)(w >> 32);
@@ -338,7 +371,7 @@ std::string disassemble(const Program& p) {
             case OP_LDC: os << "r" << d << " crow" << imm; break;
             case OP_LDK: {
                 double v;
-                std::memcpy(&v, &p.words[pc + 1], 8);
+                std::memcpy(&v, &all[pc + 1], 8);
                 os << "r" << d << " " << v;
                 ++pc;
                 break;

@@ -56,14 +56,22 @@ struct ProgramStats {
     std::uint64_t flops = 0, divs = 0, sqrts = 0, transcendentals = 0, gathers = 0, constLoads = 0, stores = 0;
 };
 
+// A program has two sections.  `loads` holds every distinct gather (LDX) and
+// per-instance constant read (LDC) of the template, each loaded once into its
+// own register before any arithmetic, so the interpreter can issue them all
+// back to back.  `words` holds the arithmetic, literal loads (LDK) and output
+// stores, ending with OP_END.
 struct Program {
+    std::vector<std::uint64_t> loads;
     std::vector<std::uint64_t> words;
     int registers = 0;
     ProgramStats stats;
 };
 
 // Compiles one kernel template.  Throws std::runtime_error on templates the
-// engine cannot execute (unknown operations, more than MAX_REGISTERS live values).
+// engine cannot execute (unknown operations, more than MAX_REGISTERS live
+// values).  Loads are deduplicated: a gather that the template reads several
+// times is loaded once; the value is the same, so results do not change.
 Program compileTemplate(const symgb_kernel_desc& k, int math);
 
 // Human-readable listing (tests and debugging).

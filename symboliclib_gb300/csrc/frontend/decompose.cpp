@@ -90,12 +90,11 @@ struct Node {
     Symbolic extractExpression(int groupId) {
         if (x.op() != NOOP) return x;
         std::vector<std::pair<Symbolic, hash_t>> stack;
-        NodeMap<std::pair<Symbolic, hash_t>> cache;
+        KeyMap<std::pair<Symbolic, hash_t>> cache;
 
         auto pre = [&](const Symbolic& y) {
-            auto itc = cache.find(y.id());
-            if (itc != cache.end()) {
-                stack.push_back(itc->second);
+            if (auto* itc = cache.find(y.id())) {
+                stack.push_back(*itc);
                 return false;
             }
             if (y.op() == FIXED) {
@@ -162,7 +161,7 @@ std::vector<ExpressionBlock> decompose(const std::vector<Symbolic>& expr, unsign
     std::vector<Node> nodes;
     nodes.reserve(5 * expr.size());
     // node identity -> (occurrence count, node index + 1)
-    std::unordered_map<long long, std::pair<unsigned, unsigned>, IdentityHash> count;
+    KeyMap<std::pair<unsigned, unsigned>> count(4 * expr.size());
     int id = 0;
 
     // 1. Count occurrences; a complex sub-expression seen twice becomes a node.
@@ -224,9 +223,17 @@ std::vector<ExpressionBlock> decompose(const std::vector<Symbolic>& expr, unsign
         node.complexity = (unsigned char)std::min(255, comp);
     }
 
-    // 4. Merge small and single-parent children, assign levels.
+    // 4. Merge small and single-parent children, assign levels.  `reachable`
+    // is a flag per node; nodes live in one array, so index order is the
+    // pointer order of the reference's std::set<ExpressionNode*>.
     std::vector<Node*> stack;
-    std::set<Node*> reachable;
+    std::vector<char> reachable(nodes.size(), 0);
+    auto insertReachable = [&](Node* n) {
+        char& f = reachable[n - nodes.data()];
+        const bool fresh = !f;
+        f = 1;
+        return fresh;
+    };
     std::vector<Node*> childStack;
     for (unsigned i : outputNodes) {
         Node* x = nodes.data() + i;
@@ -237,8 +244,8 @@ std::vector<ExpressionBlock> decompose(const std::vector<Symbolic>& expr, unsign
             Node* node = stack.back();
             stack.pop_back();
             if (node->status == FIXED_NODE) {
-                reachable.insert(node);
-            } else if (node->status != 0 || reachable.insert(node).second) {
+                insertReachable(node);
+            } else if (node->status != 0 || insertReachable(node)) {
                 childStack.clear();
                 for (auto& c : node->childs) childStack.push_back(c.second);
                 while (!childStack.empty()) {
@@ -264,7 +271,9 @@ std::vector<ExpressionBlock> decompose(const std::vector<Symbolic>& expr, unsign
     // 5. Blocks of the reachable, non-inlined nodes in node order.
     std::vector<int> blockIdMap(nodes.size(), -1);
     std::vector<ExpressionBlock> blocks;
-    for (Node* x : reachable) {
+    for (std::size_t ni = 0; ni < nodes.size(); ++ni) {
+        if (!reachable[ni]) continue;
+        Node* x = &nodes[ni];
         if (x->status == MERGED) continue;
         blockIdMap[x->id] = (int)blocks.size();
         ExpressionBlock b;

@@ -36,7 +36,8 @@ class PlanDesc(C.Structure):
 
 class Schedule(C.Structure):
     _fields_ = [("kind", C.c_int32), ("math", C.c_int32), ("threads_per_block", C.c_int32),
-                ("items_per_tile", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32)]
+                ("items_per_tile", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32),
+                ("items_per_thread", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -70,6 +71,9 @@ SYMGB_FUNCTIONS = {
     "symgb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "symgb_algorithmic_bytes": (C.c_uint64, [C.c_void_p, C.c_int]),
     "symgb_last_launch_count": (C.c_int, [C.c_void_p]),
+    "symgb_measure_fp64_rate": (C.c_int, [C.POINTER(C.c_double)]),
+    "symgb_kernel_program": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int)]),
 }
 
 _libs: dict[str, C.CDLL] = {}
@@ -205,8 +209,8 @@ class Unit:
         return cls(w.plan, w.index_data, w.out_index_data, w.const_data)
 
     def set_schedule(self, kind=SCHEDULE_PLAIN, math=MATH_FAST, threads_per_block=0, items_per_tile=0,
-                     blocks_per_sm=0, use_graph=0) -> None:
-        s = Schedule(kind, math, threads_per_block, items_per_tile, blocks_per_sm, use_graph)
+                     blocks_per_sm=0, use_graph=0, items_per_thread=1) -> None:
+        s = Schedule(kind, math, threads_per_block, items_per_tile, blocks_per_sm, use_graph, items_per_thread)
         check(self._lib.symgb_set_schedule(self.handle, C.byref(s)))
 
     def set_num_sets(self, n: int) -> None:

@@ -1,0 +1,132 @@
+"""GPU parity tests: the CUDA engine, called through the C ABI, against the
+reference's own results (golden fixtures) and the CPU oracle.
+
+Exact mode must be bit-identical for every schedule and batch size; fast mode
+(FMA contraction) must agree to 1e-12 relative per nonzero, entries below a
+floor compared against that floor: 1e-10 of the container's largest magnitude,
+and 1e-4 for the cloth Hessian, whose coupling entries are sums of terms up to
+~1e4 times larger than the result (contraction rounds those terms
+differently; an exact emulation of the FMA program gives the same error)."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden
+from symboliclib_gb300 import native
+
+import oracle.cpu as ocpu
+
+pytestmark = pytest.mark.gpu
+
+SCHEDULES = [native.SCHEDULE_PLAIN, native.SCHEDULE_LEVELS, native.SCHEDULE_PERSISTENT]
+TOL = 1e-12
+FAST_FLOOR = {"cloth": 1e-4}
+
+
+def split_inputs(w, flat):
+    out, off = [], 0
+    for a in w.inputs:
+        out.append(flat[off:off + len(a)])
+        off += len(a)
+    return out
+
+
+def rel_err(a, ref, floor_frac=1e-10):
+    floor = floor_frac * np.max(np.abs(ref))
+    return float(np.max(np.abs(a - ref) / np.maximum(np.abs(ref), floor)))
+
+
+def bits_equal(a, b):
+    return a.shape == b.shape and np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+@pytest.mark.parametrize("name,size,seed", GOLDEN_CASES)
+@pytest.mark.parametrize("kind", SCHEDULES)
+def test_exact_mode_bit_identical_to_reference(name, size, seed, kind):
+    _, inp, gold = load_golden(name, size)
+    w = native.Workload(name, size, seed)
+    u = native.Unit.from_workload(w)
+    u.set_schedule(kind=kind, math=native.MATH_EXACT)
+    for i, a in enumerate(split_inputs(w, inp)):
+        u.set_arg(i, a)
+    u.run()
+    assert bits_equal(u.get_result(0), gold)
+
+
+@pytest.mark.parametrize("name,size,seed", GOLDEN_CASES)
+@pytest.mark.parametrize("kind", SCHEDULES)
+def test_fast_mode_within_tolerance(name, size, seed, kind):
+    _, inp, gold = load_golden(name, size)
+    w = native.Workload(name, size, seed)
+    u = native.Unit.from_workload(w)
+    u.set_schedule(kind=kind, math=native.MATH_FAST)
+    for i, a in enumerate(split_inputs(w, inp)):
+        u.set_arg(i, a)
+    u.run()
+    assert rel_err(u.get_result(0), gold, FAST_FLOOR.get(name, 1e-10)) <= TOL
+
+
+@pytest.mark.parametrize("name,size,seed", [("cotan", 8, 22), ("cloth", 5, 32), ("ata", 9, 12)])
+@pytest.mark.parametrize("kind", SCHEDULES)
+@pytest.mark.parametrize("sets", [2, 7, 33, 64])
+def test_value_set_batches_match_oracle(name, size, seed, kind, sets):
+    """S value sets in one run: every set bit-identical (exact mode) to the
+    oracle evaluated on that set alone."""
+    w = native.Workload(name, size, seed)
+    u = native.Unit.from_workload(w)
+    u.set_schedule(kind=kind, math=native.MATH_EXACT)
+    u.set_num_sets(sets)
+    rng = np.random.default_rng(seed + sets)
+    per_set = [[a * (1.0 + 0.05 * rng.standard_normal(a.shape)) for a in w.inputs] for _ in range(sets)]
+    for i in range(len(w.inputs)):
+        u.set_arg(i, np.concatenate([ps[i] for ps in per_set]))
+    u.run()
+    out = u.get_result(0).reshape(sets, -1)
+    for s in (0, sets // 2, sets - 1):
+        ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, per_set[s])[0]
+        assert bits_equal(out[s], ref), f"set {s}"
+
+
+@pytest.mark.parametrize("kind", [native.SCHEDULE_PLAIN, native.SCHEDULE_LEVELS])
+def test_graph_replay_matches(kind):
+    _, inp, gold = load_golden("cloth", 5)
+    w = native.Workload("cloth", 5, 32)
+    u = native.Unit.from_workload(w)
+    u.set_schedule(kind=kind, math=native.MATH_EXACT, use_graph=1)
+    for i, a in enumerate(split_inputs(w, inp)):
+        u.set_arg(i, a)
+    for _ in range(3):
+        u.run()
+        assert bits_equal(u.get_result(0), gold)
+    assert u.last_launch_count() > 0
+
+
+@pytest.mark.parametrize("tpb", [32, 64, 256])
+@pytest.mark.parametrize("items", [1, 2, 4])
+def test_block_sizes_and_items_per_thread(tpb, items):
+    for name, size, seed in [("cotan", 8, 22), ("cloth", 5, 32)]:
+        _, inp, gold = load_golden(name, size)
+        w = native.Workload(name, size, seed)
+        u = native.Unit.from_workload(w)
+        for kind in SCHEDULES:
+            for tile in (0, 3 * tpb):
+                u.set_schedule(kind=kind, math=native.MATH_EXACT, threads_per_block=tpb, items_per_tile=tile,
+                               items_per_thread=items)
+                for i, a in enumerate(split_inputs(w, inp)):
+                    u.set_arg(i, a)
+                u.run()
+                assert bits_equal(u.get_result(0), gold), (name, kind, tile)
+
+
+def test_larger_cases_match_oracle():
+    """Sizes beyond the fixtures: engine exact mode vs the CPU oracle."""
+    for name, size, seed in [("cotan", 60, 5), ("ata", 30, 6), ("cloth", 12, 7)]:
+        w = native.Workload(name, size, seed)
+        ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
+        assert rel_err(w.numeric, ref, floor_frac=1e-4) <= TOL
+        u = native.Unit.from_workload(w)
+        for kind in SCHEDULES:
+            u.set_schedule(kind=kind, math=native.MATH_EXACT)
+            for i, a in enumerate(w.inputs):
+                u.set_arg(i, a)
+            u.run()
+            assert bits_equal(u.get_result(0), ref), (name, kind)
