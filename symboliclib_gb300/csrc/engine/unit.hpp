@@ -1,0 +1,125 @@
+// Host-side state of an engine unit, shared by the engine's translation units
+// (engine.cu: the C ABI; static_scratch.cu: the allocation-free entry point).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "device.cuh"
+#include "program.hpp"
+#include "symgb.h"
+
+namespace symgb {
+namespace engine {
+
+// Records the message returned by symgb_last_error() on this thread and
+// returns `code`.
+int setLastError(int code, const std::string& msg);
+
+struct HostKernel {
+    symgb_kernel_desc desc;
+    std::vector<symgb_node> nodes;
+    std::vector<std::int32_t> access;
+    Program prog[2];  // exact, fast
+};
+
+template <class T>
+struct DevBuf {
+    T* ptr = nullptr;
+    std::size_t count = 0;
+    ~DevBuf() { reset(); }
+    void reset() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+    cudaError_t alloc(std::size_t n) {
+        reset();
+        if (n == 0) n = 1;
+        cudaError_t e = cudaMalloc(&ptr, n * sizeof(T));
+        if (e == cudaSuccess) count = n;
+        return e;
+    }
+};
+
+}  // namespace engine
+}  // namespace symgb
+
+struct symgb_unit {
+    using HostKernel = symgb::engine::HostKernel;
+    template <class T>
+    using DevBuf = symgb::engine::DevBuf<T>;
+    // plan
+    std::vector<HostKernel> kernels;
+    std::vector<std::uint64_t> argStart, argLength, outStart, outLength;
+    std::uint64_t numTotalMemory = 0, numIndices = 0, numOutputValues = 0, numConstants = 0;
+    int threadsPerBlock = 128;
+    int numLevels = 0;
+    symgb_schedule sched{SYMGB_SCHEDULE_PLAIN, SYMGB_MATH_FAST, 0, 0, 0, 0, 1};
+    int numSets = 1;
+
+    // device state
+    bool initialized = false;
+    int device = 0;
+    int smCount = 0;
+    std::size_t smemOptin = 48 * 1024;  // max dynamic shared memory per block
+    cudaStream_t ownStream = nullptr, stream = nullptr;
+    DevBuf<double> x, c, staging, outBuf;
+    DevBuf<std::uint32_t> p, ids;
+    DevBuf<std::uint64_t> progs;
+    DevBuf<DevKernel> devKernels;
+    DevBuf<Tile> tiles;
+    DevBuf<std::uint32_t> levelSeg, kernelSeg;
+    DevBuf<BarrierState> barrier;
+    int* errorHost = nullptr;  // mapped pinned flag written by the device
+    int* errorDev = nullptr;
+    std::vector<DevKernel> hostDevKernels;
+    std::vector<std::uint32_t> hostLevelSeg, hostKernelSeg;  // tile boundaries per level / per kernel
+    std::vector<Tile> hostTiles;
+    std::uint32_t maxProgWords = 0;
+    std::size_t tilesFor = 0;  // configuration the tile table was built for
+    int tilesSets = -1, tilesItems = -1, tilesMath = -1;
+    cudaGraphExec_t graph = nullptr;
+    bool graphValid = false;
+    int lastLaunches = 0;
+    int launchesPerRun = 0;
+    unsigned long long barrierTimeoutNs = 2000000000ull;
+
+    ~symgb_unit() { release(); }
+
+    void dropGraph() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        graphValid = false;
+    }
+
+    void release() {
+        dropGraph();
+        x.reset();
+        c.reset();
+        staging.reset();
+        outBuf.reset();
+        p.reset();
+        ids.reset();
+        progs.reset();
+        devKernels.reset();
+        tiles.reset();
+        levelSeg.reset();
+        kernelSeg.reset();
+        barrier.reset();
+        if (errorHost) cudaFreeHost(errorHost);
+        errorHost = nullptr;
+        errorDev = nullptr;
+        if (ownStream) cudaStreamDestroy(ownStream);
+        ownStream = nullptr;
+        stream = nullptr;
+        initialized = false;
+    }
+
+    int mathIndex() const { return sched.math == SYMGB_MATH_EXACT ? 0 : 1; }
+    int tpb() const { return sched.threads_per_block > 0 ? sched.threads_per_block : threadsPerBlock; }
+    int items() const { return sched.items_per_thread == 2 || sched.items_per_thread == 4 ? sched.items_per_thread : 1; }
+};
+
