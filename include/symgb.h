@@ -187,6 +187,23 @@ int64_t symgb_kernel_program(symgb_unit_t u, int k, int math, uint64_t* words, u
 /* Measured FP64 FMA throughput of the current device (FLOP/s, one FMA = 2). */
 int symgb_measure_fp64_rate(double* flops_per_second);
 
+/* Allocation-free evaluation, for callers that cannot allocate device memory
+ * (a framework that owns all device memory through its own pool, or code that
+ * must not allocate once running).  It has no counterpart in the reference.
+ * The unit needs only symgb_unit_create (not symgb_init, which allocates).
+ * Tables are host pointers (as for symgb_init), inputs[i] and outputs[k] are
+ * device pointers to input container i and output container k (one value set).
+ * All working memory - x, tables, programs, tiles and barrier state - lives in
+ * one static device array of SYMGB_STATIC_SCRATCH_BYTES that every GPU loading
+ * this entry point keeps until exit; plans that need more are rejected with
+ * SYMGB_ERR_ARGUMENT.  No cudaMalloc / cudaFree or other allocating call is
+ * made.  The first call on a device looks up the array's device address, so
+ * make it before any stream capture.  Calls share the array and return when the
+ * work on `stream` is done; calls from several threads must not overlap. */
+#define SYMGB_STATIC_SCRATCH_BYTES (32ull << 20)
+int symgb_run_static(symgb_unit_t u, const uint32_t* index_data, const uint32_t* out_index_data,
+                     const double* const_data, const double* const* inputs, double* const* outputs, void* stream);
+
 /* Number of kernel launches the last run issued (graph replays count the
  * kernels inside the graph). */
 int symgb_last_launch_count(symgb_unit_t u);

@@ -71,6 +71,8 @@ SYMGB_FUNCTIONS = {
     "symgb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "symgb_algorithmic_bytes": (C.c_uint64, [C.c_void_p, C.c_int]),
     "symgb_last_launch_count": (C.c_int, [C.c_void_p]),
+    "symgb_run_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]),
     "symgb_measure_fp64_rate": (C.c_int, [C.POINTER(C.c_double)]),
     "symgb_kernel_program": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]),
