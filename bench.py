@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--schedule", default="persistent", choices=["plain", "levels", "persistent"])
     ap.add_argument("--math", default="fast", choices=["fast", "exact"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-probe", action="store_true", help="skip the FP64 peak probe (e.g. under a profiler)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     return ap.parse_args()
 
@@ -266,8 +267,9 @@ def run_engine(args):
     alg_bytes = u.algorithmic_bytes(S)
     peak, peak_kind = peaks()
     achieved = alg_bytes / t_step / 1e9
-    fp64 = C.c_double()
-    native.check(lib.symgb_measure_fp64_rate(C.byref(fp64)))
+    fp64 = C.c_double(1.25e12)  # nominal GB300 FP64 rate when the probe is skipped
+    if not args.no_fp64_probe:
+        native.check(lib.symgb_measure_fp64_rate(C.byref(fp64)))
     flops = (stats.flops + 10 * stats.divs + 10 * stats.sqrts) * S
 
     if rank != 0:
@@ -286,7 +288,8 @@ def run_engine(args):
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
                          "algorithmic_bytes_per_step": alg_bytes},
             "fp64": {"flops_per_step": flops, "achieved_tflops": flops / t_step / 1e12,
-                     "measured_peak_tflops": fp64.value / 1e12, "frac": flops / t_step / fp64.value},
+                     "peak_tflops": fp64.value / 1e12, "peak_source": "nominal" if args.no_fp64_probe else "measured",
+                     "frac": flops / t_step / fp64.value},
             "e2e": {"value": world * nnz * S / t_e2e, "unit": "nnz/s", "ms_per_step": t_e2e * 1e3,
                     "h2d_bytes_per_step": int(sum(a.nbytes for a in inputs)), "d2h_bytes_per_step": int(nnz * S * 8),
                     "max_rel_err_vs_fp64_model": e2e_err},

@@ -18,16 +18,12 @@ void collect(std::vector<std::pair<Symbolic*, std::size_t>>& out, C& c, Rest&...
 }
 }  // namespace detail
 
-// Marks the entries of the given containers as one fixed block: every distinct
-// expression (by algebraic hash) gets a fresh EXPLICIT_INTERMEDIATE variable,
-// all of them are assigned inside one BLOCK, and each entry becomes
-// FIXED(variable, block).  The decomposition never splits a fixed block, so the
-// block is evaluated as one kernel instance (reference
-// src/SymbolicUtilities.hpp:52-86).
-template <class... Conts>
-void makeFixed(Conts&... conts) {
-    std::vector<std::pair<Symbolic*, std::size_t>> data;
-    detail::collect(data, conts...);
+// Marks the given entries as one fixed block: every distinct expression (by
+// algebraic hash) gets a fresh EXPLICIT_INTERMEDIATE variable, all of them are
+// assigned inside one BLOCK, and each entry becomes FIXED(variable, block).
+// The decomposition never splits a fixed block, so the block is evaluated as
+// one kernel instance (reference src/SymbolicUtilities.hpp:52-86).
+inline void makeFixedSpans(const std::vector<std::pair<Symbolic*, std::size_t>>& data) {
     if (data.empty()) return;
     std::unordered_map<hash_t, Symbolic, IdentityHash> exprMap;
     std::vector<Symbolic> assignments;
@@ -42,6 +38,20 @@ void makeFixed(Conts&... conts) {
     Symbolic block(BLOCK, assignments);
     for (auto& d : data)
         for (std::size_t i = 0; i < d.second; ++i) d.first[i] = Symbolic(FIXED, exprMap[d.first[i].ahash()], block);
+}
+
+template <class... Conts>
+void makeFixed(Conts&... conts) {
+    std::vector<std::pair<Symbolic*, std::size_t>> data;
+    detail::collect(data, conts...);
+    makeFixedSpans(data);
+}
+
+// makeFixed over the rows of a matrix stored as a vector of rows.
+inline void makeFixedRows(std::vector<std::vector<Symbolic>>& rows) {
+    std::vector<std::pair<Symbolic*, std::size_t>> data;
+    for (auto& r : rows) data.emplace_back(r.data(), r.size());
+    makeFixedSpans(data);
 }
 
 // Evaluates an expression with values for the variables of one group

@@ -177,41 +177,54 @@ __device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t
                     for (int j = 0; j < ITEMS; ++j) REG(d, j) = v[u][j];
                 }
         }
-        // Arithmetic and stores.
+        // Arithmetic and stores.  `acc` holds the last result (per item); flag
+        // bits route single-use values through it instead of shared memory.
+        double acc[ITEMS];
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) acc[j] = 0.0;
         for (const std::uint64_t* ip = prog + nl;;) {
             const std::uint64_t w = *ip++;
             const unsigned op = (unsigned)(w & 0xff);
             const unsigned d = (unsigned)(w >> 8) & 0xff;
             const unsigned a = (unsigned)(w >> 16) & 0xff;
             const unsigned bb = (unsigned)(w >> 24) & 0xff;
+            const bool aAcc = (w & F_A_ACC) != 0, bAcc = (w & F_B_ACC) != 0, keep = (w & F_NOSTORE) == 0;
             if (op == OP_END) break;
+#define OPA(j) (aAcc ? acc[j] : REG(a, j))
+#define OPB(j) (bAcc ? acc[j] : REG(bb, j))
+#define RESULT(j, v)              \
+    {                             \
+        const double r_ = (v);    \
+        acc[j] = r_;              \
+        if (keep) REG(d, j) = r_; \
+    }
             switch (op) {
                 case OP_LDK: {
                     const double cv = __longlong_as_double((long long)*ip++);
 #pragma unroll
-                    for (int j = 0; j < ITEMS; ++j) REG(d, j) = cv;
+                    for (int j = 0; j < ITEMS; ++j) RESULT(j, cv)
                     break;
                 }
                 case OP_ST: {
-                    const std::uint64_t row = (std::uint64_t)(unsigned)(w >> 32);
+                    const std::uint64_t row = (std::uint64_t)((w >> 32) & 0xffffff);
 #pragma unroll
                     for (int j = 0; j < ITEMS; ++j)
-                        if (valid[j]) A.xw[(k.yoff + row * k.n + ii[j]) * S + ss[j]] = REG(a, j);
+                        if (valid[j]) A.xw[(k.yoff + row * k.n + ii[j]) * S + ss[j]] = OPA(j);
                     break;
                 }
 #define BIN(OPC, EXPR)                                                 \
     case OPC: {                                                        \
         _Pragma("unroll") for (int j = 0; j < ITEMS; ++j) {            \
-            const double x1 = REG(a, j), x2 = REG(bb, j);              \
-            REG(d, j) = (EXPR);                                        \
+            const double x1 = OPA(j), x2 = OPB(j);                     \
+            RESULT(j, (EXPR))                                          \
         }                                                              \
         break;                                                         \
     }
 #define UN(OPC, EXPR)                                                  \
     case OPC: {                                                        \
         _Pragma("unroll") for (int j = 0; j < ITEMS; ++j) {            \
-            const double x1 = REG(a, j);                               \
-            REG(d, j) = (EXPR);                                        \
+            const double x1 = OPA(j);                                  \
+            RESULT(j, (EXPR))                                          \
         }                                                              \
         break;                                                         \
     }
@@ -237,12 +250,19 @@ __device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t
                 case OP_FMA: {
                     const unsigned cr = (unsigned)(w >> 32) & 0xff;
                     const int fl = (int)((w >> 40) & 0x3);
+                    const bool cAcc = (w & F_C_ACC) != 0;
 #pragma unroll
-                    for (int j = 0; j < ITEMS; ++j) REG(d, j) = dfma(REG(a, j), REG(bb, j), REG(cr, j), fl);
+                    for (int j = 0; j < ITEMS; ++j) {
+                        const double x3 = cAcc ? acc[j] : REG(cr, j);
+                        RESULT(j, dfma(OPA(j), OPB(j), x3, fl))
+                    }
                     break;
                 }
                 default: break;
             }
+#undef OPA
+#undef OPB
+#undef RESULT
         }
 #undef REG
     }

@@ -68,11 +68,68 @@ public:
             statement(root_);
         }
         prog_.words.push_back(encode(OP_END, 0, 0, 0, 0));
+        chainThroughAccumulator(prog_.words);
         prog_.registers = maxReg_;
         return std::move(prog_);
     }
 
 private:
+    struct Decoded {
+        std::size_t pos;  // word index
+        int op, d, a, b, c;
+        bool defines;
+        int useA, useB, useC;  // register read through operand a / b / FMA addend, or -1
+    };
+
+    static Decoded decode(const std::vector<std::uint64_t>& w, std::size_t pos) {
+        const std::uint64_t x = w[pos];
+        Decoded I{pos, (int)(x & 0xff), (int)((x >> 8) & 0xff), (int)((x >> 16) & 0xff), (int)((x >> 24) & 0xff),
+                  (int)((x >> 32) & 0xff), false, -1, -1, -1};
+        switch (I.op) {
+            case OP_LDK: I.defines = true; break;
+            case OP_ST: I.useA = I.a; break;
+            case OP_ADD: case OP_SUB: case OP_MUL: case OP_DIV: case OP_POW:
+                I.defines = true; I.useA = I.a; I.useB = I.b; break;
+            case OP_FMA: I.defines = true; I.useA = I.a; I.useB = I.b; I.useC = I.c; break;
+            case OP_END: break;
+            default: I.defines = true; I.useA = I.a; break;  // unary
+        }
+        return I;
+    }
+
+    // A value whose only reader is the next instruction stays in the
+    // accumulator: its producer skips the register-file write and the reader
+    // takes the operand from the accumulator.  Values and their order are
+    // unchanged, only where they are kept.
+    static void chainThroughAccumulator(std::vector<std::uint64_t>& w) {
+        std::vector<Decoded> ins;
+        for (std::size_t pos = 0; pos < w.size();) {
+            ins.push_back(decode(w, pos));
+            pos += ins.back().op == OP_LDK ? 2 : 1;
+        }
+        for (std::size_t i = 0; i + 1 < ins.size(); ++i) {
+            const Decoded& I = ins[i];
+            if (!I.defines) continue;
+            const int r = I.d;
+            int readers = 0;
+            std::size_t first = 0;
+            for (std::size_t j = i + 1; j < ins.size(); ++j) {
+                const Decoded& J = ins[j];
+                if (J.useA == r || J.useB == r || J.useC == r) {
+                    if (!readers) first = j;
+                    ++readers;
+                }
+                if (J.defines && J.d == r) break;
+            }
+            if (readers != 1 || first != i + 1) continue;
+            const Decoded& J = ins[i + 1];
+            w[I.pos] |= F_NOSTORE;
+            if (J.useA == r) w[J.pos] |= F_A_ACC;
+            if (J.useB == r) w[J.pos] |= F_B_ACC;
+            if (J.useC == r) w[J.pos] |= F_C_ACC;
+        }
+    }
+
     const symgb_node& node(int j) const { return k_.nodes[j]; }
 
     // Key of a load leaf: kind (1 gather, 2 constant) in bits 62-63.
@@ -325,6 +382,7 @@ private:
             const symgb_node& out = node(kids_[j][0]);
             if (out.op != N_VAR || out.b != G_OUTPUT) throw std::runtime_error("ASSIGN to a non-output");
             if (out.a < 0 || (std::uint32_t)out.a >= k_.num_output_rows) throw std::runtime_error("output row out of range");
+            if ((std::uint32_t)out.a >= ST_ROW_LIMIT) throw std::runtime_error("more than 2^24 output rows");
             Val v = expr(kids_[j][1]);
             emit(encode(OP_ST, 0, v.reg, 0, (std::uint32_t)out.a));
             ++prog_.stats.stores;
@@ -376,10 +434,11 @@ std::string disassemble(const Program& p) {
                 ++pc;
                 break;
             }
-            case OP_ST: os << "y" << imm << " r" << a; break;
+            case OP_ST: os << "y" << ((w >> 32) & 0xffffff) << " r" << a; break;
             case OP_FMA: os << "r" << d << " r" << a << " r" << b << " r" << (imm & 0xff) << " f" << (imm >> 8); break;
             default: os << "r" << d << " r" << a << " r" << b;
         }
+        if (w >> 56) os << " acc" << (w >> 56);
         os << "\n";
     }
     return os.str();

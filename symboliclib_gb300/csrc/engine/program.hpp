@@ -52,6 +52,16 @@ constexpr int FMA_NEG_PRODUCT = 1;
 constexpr int FMA_NEG_ADDEND = 2;
 constexpr int MAX_REGISTERS = 255;
 
+// Accumulator flags, bits 56-63 of a compute word.  The interpreter keeps the
+// result of every instruction in a hardware register (the accumulator); a
+// value consumed only by the very next instruction is passed there instead of
+// through the shared-memory register file.
+constexpr std::uint64_t F_A_ACC = 1ull << 56;    // operand a is the accumulator
+constexpr std::uint64_t F_B_ACC = 2ull << 56;    // operand b is the accumulator
+constexpr std::uint64_t F_C_ACC = 4ull << 56;    // FMA addend is the accumulator
+constexpr std::uint64_t F_NOSTORE = 8ull << 56;  // result only in the accumulator
+constexpr std::uint32_t ST_ROW_LIMIT = 1u << 24; // OP_ST row field: bits 32-55
+
 struct ProgramStats {
     std::uint64_t flops = 0, divs = 0, sqrts = 0, transcendentals = 0, gathers = 0, constLoads = 0, stores = 0;
 };

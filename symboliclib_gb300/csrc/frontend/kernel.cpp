@@ -17,38 +17,42 @@ namespace symgb {
 
 namespace {
 
-hash_t hashInstances(const std::vector<Symbolic>& x) {
-    std::vector<hash_t> hs;
-    hs.reserve(x.size());
-    for (auto& xi : x) hs.push_back(xi.ahash());
-    return hashVector(hs);
-}
-
-// The lockstep cursor: the same child position across all instances.
+// The lockstep cursor: the same child position across all instances.  It
+// holds pointers to the instances' handles (kept alive by the instance list),
+// so walking a template over many instances copies no reference counts.
 struct Lockstep {
-    std::vector<Symbolic> x;
+    std::vector<const Symbolic*> x;
     hash_t h = 0;
     unsigned childCounter = 0;
 
-    explicit Lockstep(const std::vector<Symbolic>& xs) : x(xs) { init(); }
-    Lockstep(const std::vector<Symbolic>& parents, unsigned child) {
-        x.reserve(parents.size());
-        for (auto& p : parents) x.push_back(p[child]);
+    explicit Lockstep(const std::vector<Symbolic>& xs) {
+        x.reserve(xs.size());
+        for (auto& s : xs) x.push_back(&s);
         init();
     }
-    void init() {
-        if (!x.empty()) h = hashInstances(x);
+    Lockstep(const std::vector<const Symbolic*>& parents, unsigned child) {
+        x.reserve(parents.size());
+        for (auto* p : parents) x.push_back(&(*p)[child]);
+        init();
     }
-    unsigned numChilds() const { return x.empty() ? 0 : x.front().numChilds(); }
-    OpType op() const { return x.empty() ? NOOP : x.front().op(); }
-    bool visit() { return childCounter++ == x.front().numChilds(); }
+    // Hash of the instances' algebraic hashes (reference ComputeKernel.cpp:14-20).
+    void init() {
+        if (x.empty()) return;
+        std::vector<hash_t> hs;
+        hs.reserve(x.size());
+        for (auto* xi : x) hs.push_back(xi->ahash());
+        h = hashVector(hs);
+    }
+    unsigned numChilds() const { return x.empty() ? 0 : x.front()->numChilds(); }
+    OpType op() const { return x.empty() ? NOOP : x.front()->op(); }
+    bool visit() { return childCounter++ == x.front()->numChilds(); }
 
     // The variable of every instance.  The table is never collapsed to a single
     // entry: the reference's all-identical test (ComputeKernel.cpp:92) is
     // inverted and always fails.
     std::vector<std::array<int, 2>> variables() const {
         std::vector<std::array<int, 2>> v(x.size());
-        for (std::size_t i = 0; i < x.size(); ++i) v[i] = x[i].variable();
+        for (std::size_t i = 0; i < x.size(); ++i) v[i] = x[i]->variable();
         return v;
     }
     // The constant of every instance, or one value if all are equal.
@@ -56,7 +60,7 @@ struct Lockstep {
         std::vector<double> v(x.size());
         bool allEqual = true;
         for (std::size_t i = 0; i < x.size(); ++i) {
-            v[i] = x[i].constant();
+            v[i] = x[i]->constant();
             if (allEqual && v[0] != v[i]) allEqual = false;
         }
         if (allEqual) v.resize(1);

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdint>
 #include <map>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -581,6 +582,172 @@ CSC<NT> clothMatrix(const ClothRest& r, const std::vector<NT>& X, const std::vec
         A.colPtr[c + 1] = (int)A.values.size();
     }
     return A;
+}
+
+// ---------------------------------------------------------------- workload 5: Neo-Hookean tets
+
+// Tetrahedral mesh of a cells^3 cube grid at unit spacing, 5 tets per cell
+// (the split alternates with cell parity so faces match), with rest-shape
+// quantities.  The deformed state compresses z by 10% and adds uniform noise.
+struct TetMesh {
+    int nv = 0;
+    std::vector<double> rest;                 // nv x 3 column-major
+    std::vector<std::array<int, 4>> T;
+    std::vector<std::array<double, 9>> Dminv; // per tet, 3x3 row-major inverse of [x1-x0, x2-x0, x3-x0]
+    std::vector<double> volume;               // per tet, rest volume
+    double mu = 1.0, lambda = 10.0;
+};
+
+inline TetMesh tetMesh(int cells) {
+    TetMesh m;
+    const int s = cells + 1;
+    m.nv = s * s * s;
+    m.rest.assign(3 * (std::size_t)m.nv, 0.0);
+    auto vid = [&](int i, int j, int k) { return i + s * (j + s * k); };
+    for (int k = 0; k < s; ++k)
+        for (int j = 0; j < s; ++j)
+            for (int i = 0; i < s; ++i) {
+                const int v = vid(i, j, k);
+                m.rest[v] = i;
+                m.rest[v + m.nv] = j;
+                m.rest[v + 2 * (std::size_t)m.nv] = k;
+            }
+    static const int split[5][4] = {{0, 1, 2, 4}, {3, 2, 1, 7}, {5, 4, 7, 1}, {6, 7, 4, 2}, {1, 2, 4, 7}};
+    for (int k = 0; k < cells; ++k)
+        for (int j = 0; j < cells; ++j)
+            for (int i = 0; i < cells; ++i) {
+                const int flip = (i + j + k) & 1;
+                for (const auto& t : split) {
+                    std::array<int, 4> tet;
+                    for (int a = 0; a < 4; ++a) {
+                        const int c = t[a] ^ flip;  // mirror the split in x for odd cells
+                        tet[a] = vid(i + (c & 1), j + ((c >> 1) & 1), k + ((c >> 2) & 1));
+                    }
+                    double D[9];
+                    for (int r = 0; r < 3; ++r)
+                        for (int c = 0; c < 3; ++c)
+                            D[3 * r + c] = m.rest[tet[c + 1] + r * (std::size_t)m.nv] - m.rest[tet[0] + r * (std::size_t)m.nv];
+                    double det = D[0] * (D[4] * D[8] - D[5] * D[7]) - D[1] * (D[3] * D[8] - D[5] * D[6]) +
+                                 D[2] * (D[3] * D[7] - D[4] * D[6]);
+                    if (det < 0) {
+                        std::swap(tet[1], tet[2]);
+                        for (int r = 0; r < 3; ++r) std::swap(D[3 * r + 0], D[3 * r + 1]);
+                        det = -det;
+                    }
+                    std::array<double, 9> inv;
+                    inv[0] = (D[4] * D[8] - D[5] * D[7]) / det;
+                    inv[1] = (D[2] * D[7] - D[1] * D[8]) / det;
+                    inv[2] = (D[1] * D[5] - D[2] * D[4]) / det;
+                    inv[3] = (D[5] * D[6] - D[3] * D[8]) / det;
+                    inv[4] = (D[0] * D[8] - D[2] * D[6]) / det;
+                    inv[5] = (D[2] * D[3] - D[0] * D[5]) / det;
+                    inv[6] = (D[3] * D[7] - D[4] * D[6]) / det;
+                    inv[7] = (D[1] * D[6] - D[0] * D[7]) / det;
+                    inv[8] = (D[0] * D[4] - D[1] * D[3]) / det;
+                    m.T.push_back(tet);
+                    m.Dminv.push_back(inv);
+                    m.volume.push_back(det / 6.0);
+                }
+            }
+    return m;
+}
+
+inline std::vector<double> tetState(const TetMesh& m, std::uint64_t seed) {
+    Rng rng(seed);
+    std::vector<double> X(m.rest);
+    for (int v = 0; v < m.nv; ++v) X[v + 2 * (std::size_t)m.nv] *= 0.9;
+    for (auto& x : X) x += rng.uniform(-0.01, 0.01);
+    return X;
+}
+
+// Per-tet energy V0 * psi(F), F = Ds Dm^-1, with the log-free Neo-Hookean
+// psi = mu/2 (tr(F^T F) - 3) - mu (J - 1) + lambda/2 (J - 1)^2, J = det F
+// (zero energy and stress at rest; no logarithm, whose derivative rule the
+// symbolic differentiation does not have).
+template <class NT>
+std::vector<NT> neoHookeanEnergies(const TetMesh& m, const std::vector<NT>& X) {
+    std::vector<NT> E;
+    E.reserve(m.T.size());
+    const std::size_t n = m.nv;
+    for (std::size_t t = 0; t < m.T.size(); ++t) {
+        const auto& tet = m.T[t];
+        const auto& Mi = m.Dminv[t];
+        NT Ds[3][3], F[3][3];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) Ds[r][c] = X[tet[c + 1] + r * n] - X[tet[0] + r * n];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) F[r][c] = Ds[r][0] * NT(Mi[c]) + Ds[r][1] * NT(Mi[3 + c]) + Ds[r][2] * NT(Mi[6 + c]);
+        NT Ic = F[0][0] * F[0][0];
+        for (int q = 1; q < 9; ++q) Ic = Ic + F[q / 3][q % 3] * F[q / 3][q % 3];
+        const NT J = F[0][0] * (F[1][1] * F[2][2] - F[1][2] * F[2][1]) - F[0][1] * (F[1][0] * F[2][2] - F[1][2] * F[2][0]) +
+                     F[0][2] * (F[1][0] * F[2][1] - F[1][1] * F[2][0]);
+        const NT Jm1 = J - NT(1.0);
+        const NT psi = NT(0.5 * m.mu) * (Ic - NT(3.0)) - NT(m.mu) * Jm1 + NT(0.5 * m.lambda) * (Jm1 * Jm1);
+        E.push_back(NT(m.volume[t]) * psi);
+    }
+    return E;
+}
+
+// Symmetric Hessian from upper-triangle (row, col, value) entries: each
+// off-diagonal entry is also added transposed, duplicates summed in order.
+template <class NT>
+CSC<NT> symmetricFromUpper(int n, const std::vector<std::tuple<int, int, NT>>& upper) {
+    std::vector<Triplet<NT>> t;
+    t.reserve(2 * upper.size());
+    for (const auto& e : upper) t.push_back({std::get<0>(e), std::get<1>(e), std::get<2>(e)});
+    for (const auto& e : upper)
+        if (std::get<0>(e) != std::get<1>(e)) t.push_back({std::get<1>(e), std::get<0>(e), std::get<2>(e)});
+    return assemble(n, n, t);
+}
+
+// Analytic FP64 Hessian of the same energy (the numeric oracle of workload 5):
+// d2psi/dF_rc dF_pq = mu d_rp d_cq + lambda C_rc C_pq + (lambda (J-1) - mu) e_rpb e_cqe F_be,
+// C = cof(F), mapped to the tet's 12 coordinates through dF_rc/dx_(v,d) = d_rd G_vc.
+inline std::vector<std::tuple<int, int, double>> neoHookeanHessianUpper(const TetMesh& m, const std::vector<double>& X) {
+    std::vector<std::tuple<int, int, double>> out;
+    const std::size_t n = m.nv;
+    auto eps = [](int a, int b, int c) { return (a == b || b == c || a == c) ? 0 : (((b - a + 3) % 3 == 1) ? 1 : -1); };
+    for (std::size_t t = 0; t < m.T.size(); ++t) {
+        const auto& tet = m.T[t];
+        const auto& Mi = m.Dminv[t];
+        double Ds[3][3], F[3][3], C[3][3], G[4][3];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) Ds[r][c] = X[tet[c + 1] + r * n] - X[tet[0] + r * n];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) F[r][c] = Ds[r][0] * Mi[c] + Ds[r][1] * Mi[3 + c] + Ds[r][2] * Mi[6 + c];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c)
+                C[r][c] = F[(r + 1) % 3][(c + 1) % 3] * F[(r + 2) % 3][(c + 2) % 3] -
+                          F[(r + 1) % 3][(c + 2) % 3] * F[(r + 2) % 3][(c + 1) % 3];
+        const double J = F[0][0] * C[0][0] + F[0][1] * C[0][1] + F[0][2] * C[0][2];
+        for (int c = 0; c < 3; ++c) {
+            G[0][c] = -(Mi[c] + Mi[3 + c] + Mi[6 + c]);
+            for (int v = 1; v < 4; ++v) G[v][c] = Mi[3 * (v - 1) + c];
+        }
+        double HF[9][9];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c)
+                for (int p = 0; p < 3; ++p)
+                    for (int q = 0; q < 3; ++q) {
+                        double dC = 0.0;
+                        for (int b = 0; b < 3; ++b)
+                            for (int e = 0; e < 3; ++e) dC += eps(r, p, b) * eps(c, q, e) * F[b][e];
+                        HF[3 * r + c][3 * p + q] = m.mu * (r == p && c == q) + m.lambda * C[r][c] * C[p][q] +
+                                                   (m.lambda * (J - 1.0) - m.mu) * dC;
+                    }
+        for (int v = 0; v < 4; ++v)
+            for (int d = 0; d < 3; ++d)
+                for (int w = 0; w < 4; ++w)
+                    for (int e = 0; e < 3; ++e) {
+                        const int gi = tet[v] + d * (int)n, gj = tet[w] + e * (int)n;
+                        if (gi > gj) continue;
+                        double h = 0.0;
+                        for (int c = 0; c < 3; ++c)
+                            for (int q = 0; q < 3; ++q) h += G[v][c] * G[w][q] * HF[3 * d + c][3 * e + q];
+                        out.emplace_back(gi, gj, m.volume[t] * h);
+                    }
+    }
+    return out;
 }
 
 }  // namespace symgb_workloads

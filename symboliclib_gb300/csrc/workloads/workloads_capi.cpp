@@ -8,6 +8,7 @@
 #include <sstream>
 #include <string>
 
+#include "symgb/differentiation.hpp"
 #include "symgb/frontend.hpp"
 #include "symgb/plan_image.hpp"
 #include "symgb/utilities.hpp"
@@ -98,6 +99,18 @@ int symgbw_build(const char* name, int size, unsigned long long seed, int vector
             w->inputs.push_back(vel);
             w->numeric = clothMatrix(r, X, vel, NoFix()).values;
             w->outputs = A.nnz();
+        } else if (n == "neohookean") {
+            TetMesh m = tetMesh(size);
+            std::vector<double> X = tetState(m, seed);
+            auto XS = variables(X.size(), 0);
+            auto E = neoHookeanEnergies(m, XS);
+            auto upper = symgb::hessianSparse(symgb::Symbolic(symgb::ADD, E), XS);
+            CSC<symgb::Symbolic> H = symmetricFromUpper((int)X.size(), upper);
+            pb.addContainer(XS.data(), XS.size());
+            pb.addContainer(H.values.data(), H.values.size());
+            w->inputs.push_back(X);
+            w->numeric = symmetricFromUpper((int)X.size(), neoHookeanHessianUpper(m, X)).values;
+            w->outputs = H.nnz();
         } else {
             g_err = "unknown workload " + n;
             return -1;

@@ -13,6 +13,7 @@
 // See make_golden.sh for the build and run recipe.
 #include "ComputeUnit.hpp"
 #include "Symbolic.hpp"
+#include "SymbolicDifferentiation.hpp"
 #include "SymbolicUtilities.hpp"
 
 #include <cstdio>
@@ -211,6 +212,14 @@ int main(int argc, char** argv) {
         std::vector<double> all(X);
         all.insert(all.end(), vel.begin(), vel.end());
         run(out, A.values, all, {X, vel}, {XS, VS});
+    } else if (w == "neohookean") {
+        TetMesh m = tetMesh(size);
+        std::vector<double> X = tetState(m, seed);
+        auto XS = variables(X.size(), 0);
+        auto E = neoHookeanEnergies(m, XS);
+        auto upper = Sym::hessianSparse(Sym::Symbolic(Sym::ADD, E), XS);
+        CSC<Sym::Symbolic> H = symmetricFromUpper((int)X.size(), upper);
+        run(out, H.values, X, {X}, {XS});
     } else {
         std::fprintf(stderr, "unknown workload %s\n", w.c_str());
         return 2;

@@ -17,7 +17,7 @@ trap 'rm -rf "$WORK"' EXIT
 cd "$WORK"
 export PATH="$ROOT/oracle/_ref/bin:$PATH" SYMREF_STRICT=1
 # workload size seed
-for spec in "ata 6 11" "ata 9 12" "cotan 5 21" "cotan 8 22" "cloth 3 31" "cloth 5 32"; do
+for spec in "ata 6 11" "ata 9 12" "cotan 5 21" "cotan 8 22" "cloth 3 31" "cloth 5 32" "neohookean 1 41" "neohookean 2 42"; do
   set -- $spec
   "$OUTBIN" "$HERE" "$1" "$2" "$3" > /dev/null
 done

@@ -1,0 +1,33 @@
+"""The C++ API (include/symgb/ComputeUnit.hpp, differentiation.hpp) compiled
+into a program: the reference Tutorial's known answers on the CPU, and a
+ComputeUnit compile/execute/getResults round trip on the GPU."""
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from conftest import ROOT
+from symboliclib_gb300 import build
+
+SRC = ROOT / "tests" / "cpp" / "tutorial.cpp"
+
+
+@pytest.fixture(scope="module")
+def tutorial_binary():
+    out = build.OBJ / "tutorial_test"
+    lib = build.LIB
+    cmd = ["g++", "-std=c++17", "-O1", "-ffp-contract=off", f"-I{ROOT / 'include'}", str(SRC), "-o", str(out),
+           f"-L{lib}", "-lsymgb", f"-Wl,-rpath,{lib}"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return out
+
+
+def test_tutorial_known_answers(tutorial_binary):
+    r = subprocess.run([str(tutorial_binary)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+@pytest.mark.gpu
+def test_compute_unit_round_trip(tutorial_binary):
+    r = subprocess.run([str(tutorial_binary), "--gpu"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
