@@ -105,6 +105,8 @@ typedef struct symgb_schedule {
     int32_t blocks_per_sm;      /* persistent grid: CTAs per SM (0 = occupancy maximum) */
     int32_t use_graph;          /* capture run() into a CUDA graph and replay it */
     int32_t items_per_thread;   /* work items per thread per pass: 1, 2 or 4 (0 = 1) */
+    int32_t fusion_depth;       /* LEVELS: consecutive levels per launch (0/1 = one level; a
+                                   group of several levels is one cooperative launch) */
 } symgb_schedule;
 
 /* --- the reference's generated-library calls, per unit ----------------------- */
@@ -159,6 +161,32 @@ int symgb_run_async(symgb_unit_t u);
 int symgb_set_arg_sets_device(symgb_unit_t u, const double* d, int i);
 int symgb_get_result_sets_device(symgb_unit_t u, double* d, int k);
 int symgb_synchronize(symgb_unit_t u);
+
+/* Batches of units (many patterns of uneven size): one evaluation of every
+ * unit, each with its own schedule and value sets, captured into one CUDA graph
+ * whose branches (`streams` of them, units assigned round-robin) run
+ * concurrently.  Units must be initialized; their inputs are set as usual. */
+typedef struct symgb_batch* symgb_batch_t;
+int symgb_batch_create(symgb_unit_t* units, int n, int streams, symgb_batch_t* out);
+int symgb_batch_run(symgb_batch_t b);                        /* replay and wait */
+int symgb_batch_run_async(symgb_batch_t b, void* stream);    /* replay on `stream` (0 = own) */
+int symgb_batch_launch_count(symgb_batch_t b);               /* kernels in the graph */
+void symgb_batch_destroy(symgb_batch_t b);
+
+/* Learned schedule cost model: an FP32 MLP (inputs -> hidden -> hidden -> 1,
+ * ReLU) trained and evaluated on the GPU by the engine's own kernels.  X is
+ * row-major [n][inputs] in host memory, y [n].  Parameters are flattened as
+ * W1 (inputs x hidden), b1, W2 (hidden x hidden), b2, W3 (hidden), b3.
+ * Training minimises the mean squared error with Adam over the full batch. */
+typedef struct symgb_mlp* symgb_mlp_t;
+int symgb_mlp_create(int inputs, int hidden, unsigned long long seed, symgb_mlp_t* out);
+int symgb_mlp_num_params(symgb_mlp_t net);
+int symgb_mlp_get_params(symgb_mlp_t net, float* params);
+int symgb_mlp_set_params(symgb_mlp_t net, const float* params);
+int symgb_mlp_forward(symgb_mlp_t net, const float* X, int n, float* y);
+int symgb_mlp_gradient(symgb_mlp_t net, const float* X, const float* y, int n, float* grad, float* loss);
+int symgb_mlp_train(symgb_mlp_t net, const float* X, const float* y, int n, int epochs, float lr, float* loss);
+void symgb_mlp_destroy(symgb_mlp_t net);
 
 /* Plan statistics (host side, no device needed). */
 typedef struct symgb_stats {

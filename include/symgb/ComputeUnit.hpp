@@ -150,7 +150,7 @@ public:
         close();
         check(symgb_unit_create(&image_.desc, &unit_));
         symgb_schedule s{device_.schedule, device_.math, (int)(device_.numThreads % 32 ? 0 : device_.numThreads), 0, 0, 0,
-                         device_.itemsPerThread};
+                         device_.itemsPerThread, 0};
         check(symgb_set_schedule(unit_, &s));
         check(symgb_set_num_sets(unit_, device_.valueSets));
         check(symgb_init(unit_, image_.indexData.data(), image_.outIndexData.data(), image_.constData.data()));

@@ -12,6 +12,7 @@
 #include <array>
 #include <cstddef>
 #include <ostream>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -77,6 +78,14 @@ int appendTransposed(const std::vector<std::vector<T>>& src, std::vector<T>& dst
         for (auto& s : src) out = std::copy_n(s.begin() + packLength * i, packLength, out);
     return (int)packLength;
 }
+
+// Thrown when the blocks given to a ComputeKernel are not structurally
+// identical.  The reference groups blocks by (structure hash, level), and in
+// rare cases two different structures share that key; the reference then
+// fails its assertion in the kernel constructor (ComputeKernel.cpp:166).
+struct GroupMismatch : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
 
 // One group of structurally identical blocks: a template expression over
 // per-instance tables (reference src/ComputeKernel.cpp:27-268).

@@ -230,13 +230,21 @@ int enqueueRun(symgb_unit* u) {
             break;
         }
         case SYMGB_SCHEDULE_LEVELS: {
+            // Consecutive levels in groups of `fusion_depth`; a group of several
+            // levels is one cooperative launch with grid barriers between them.
             A.segments = u->levelSeg.ptr;
-            for (int L = 0; L < u->numLevels; ++L) {
-                const std::uint32_t nt = u->hostLevelSeg[L + 1] - u->hostLevelSeg[L];
-                if (!nt) continue;
+            const int depth = std::max(1, u->sched.fusion_depth);
+            for (int L = 0; L < u->numLevels; L += depth) {
+                const int L1 = std::min(u->numLevels, L + depth);
+                std::uint32_t maxTiles = 0, regs = 1;
+                for (int q = L; q < L1; ++q) {
+                    maxTiles = std::max(maxTiles, u->hostLevelSeg[q + 1] - u->hostLevelSeg[q]);
+                    regs = std::max(regs, maxRegs(u, q));
+                }
+                if (!maxTiles) continue;
                 A.segBegin = L;
-                A.segEnd = L + 1;
-                if (int e = launch(false, maxRegs(u, L), nt, false)) return e;
+                A.segEnd = L1;
+                if (int e = launch(L1 - L > 1, regs, maxTiles, L1 - L > 1)) return e;
             }
             break;
         }
@@ -259,7 +267,7 @@ int enqueueRun(symgb_unit* u) {
 
 int runAsync(symgb_unit* u) {
     if (!u->initialized) return fail(SYMGB_ERR_STATE, "run before init");
-    if (u->sched.use_graph && u->sched.kind != SYMGB_SCHEDULE_PERSISTENT) {
+    if (u->sched.use_graph) {
         if (!u->graphValid) {
             if (int e = buildTiles(u)) return e;
             // smem attributes must be set outside capture
@@ -507,7 +515,8 @@ int symgb_set_schedule(symgb_unit_t u, const symgb_schedule* s) {
     if (s->kind < 0 || s->kind > 2 || s->math < 0 || s->math > 1) return fail(SYMGB_ERR_ARGUMENT, "bad schedule");
     if (s->items_per_thread != 0 && s->items_per_thread != 1 && s->items_per_thread != 2 && s->items_per_thread != 4)
         return fail(SYMGB_ERR_ARGUMENT, "items_per_thread must be 1, 2 or 4");
-    if (s->items_per_tile < 0 || s->blocks_per_sm < 0) return fail(SYMGB_ERR_ARGUMENT, "negative schedule parameter");
+    if (s->items_per_tile < 0 || s->blocks_per_sm < 0 || s->fusion_depth < 0)
+        return fail(SYMGB_ERR_ARGUMENT, "negative schedule parameter");
     if (s->threads_per_block < 0 || s->threads_per_block > 1024 || (s->threads_per_block % 32))
         return fail(SYMGB_ERR_ARGUMENT, "threads_per_block must be a multiple of 32 up to 1024");
     const bool mathChanged = s->math != u->sched.math;
@@ -583,6 +592,93 @@ uint64_t symgb_algorithmic_bytes(symgb_unit_t u, int num_sets) {
 }
 
 int symgb_last_launch_count(symgb_unit_t u) { return u ? u->lastLaunches : 0; }
+
+struct symgb_batch {
+    std::vector<symgb_unit_t> units;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int launches = 0;
+    ~symgb_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+int symgb_batch_create(symgb_unit_t* units, int n, int streams, symgb_batch_t* out) {
+    if (!out || !units || n <= 0) return fail(SYMGB_ERR_ARGUMENT, "empty batch");
+    *out = nullptr;
+    streams = std::max(1, std::min(streams, 32));
+    std::unique_ptr<symgb_batch> b(new symgb_batch());
+    for (int i = 0; i < n; ++i) {
+        if (!units[i] || !units[i]->initialized) return fail(SYMGB_ERR_STATE, "batch unit not initialized");
+        if (int e = buildTiles(units[i])) return e;  // no allocation may happen inside the capture
+        b->units.push_back(units[i]);
+    }
+    SYMGB_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    std::vector<cudaStream_t> branch(streams);
+    std::vector<cudaEvent_t> done(streams);
+    cudaEvent_t fork;
+    SYMGB_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    for (int k = 0; k < streams; ++k) {
+        SYMGB_CUDA(cudaStreamCreateWithFlags(&branch[k], cudaStreamNonBlocking));
+        SYMGB_CUDA(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming));
+    }
+    // Fork: every branch waits on the capture stream; units go round-robin.
+    int err = SYMGB_OK;
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        err = fail(SYMGB_ERR_CUDA, "batch: begin capture failed");
+    } else {
+        cudaEventRecord(fork, b->stream);
+        for (int k = 0; k < streams; ++k) cudaStreamWaitEvent(branch[k], fork, 0);
+        for (int i = 0; i < n && !err; ++i) {
+            symgb_unit* u = b->units[i];
+            cudaStream_t saved = u->stream;
+            u->stream = branch[i % streams];
+            err = enqueueRun(u);
+            u->stream = saved;
+            b->launches += u->launchesPerRun;
+        }
+        for (int k = 0; k < streams; ++k) {
+            cudaEventRecord(done[k], branch[k]);
+            cudaStreamWaitEvent(b->stream, done[k], 0);
+        }
+        const cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
+        if (!err && ce != cudaSuccess) err = fail(SYMGB_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(ce));
+    }
+    if (!err && cudaGraphInstantiate(&b->exec, graph, 0) != cudaSuccess) err = fail(SYMGB_ERR_CUDA, "batch: graph instantiation failed");
+    if (graph) cudaGraphDestroy(graph);
+    cudaEventDestroy(fork);
+    for (int k = 0; k < streams; ++k) {
+        cudaEventDestroy(done[k]);
+        cudaStreamDestroy(branch[k]);
+    }
+    if (err) return err;
+    *out = b.release();
+    return SYMGB_OK;
+}
+
+int symgb_batch_run_async(symgb_batch_t b, void* stream) {
+    if (!b) return fail(SYMGB_ERR_ARGUMENT, "null batch");
+    SYMGB_CUDA(cudaGraphLaunch(b->exec, stream ? (cudaStream_t)stream : b->stream));
+    return SYMGB_OK;
+}
+
+int symgb_batch_run(symgb_batch_t b) {
+    if (int e = symgb_batch_run_async(b, nullptr)) return e;
+    SYMGB_CUDA(cudaStreamSynchronize(b->stream));
+    for (auto* u : b->units)
+        if (int e = checkDeviceError(u)) return e;
+    return SYMGB_OK;
+}
+
+int symgb_batch_launch_count(symgb_batch_t b) { return b ? b->launches : 0; }
+
+void symgb_batch_destroy(symgb_batch_t b) {
+    if (!b) return;
+    cudaStreamSynchronize(b->stream);
+    delete b;
+}
 
 int64_t symgb_kernel_program(symgb_unit_t u, int k, int math, uint64_t* words, uint64_t cap, int* registers,
                              int* num_loads) {

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <functional>
 #include <sstream>
 #include <stdexcept>
 #include <unordered_map>
@@ -61,12 +62,7 @@ public:
                 prog_.loads.push_back(encode(OP_LDC, d, 0, 0, row));
             }
         }
-        const symgb_node& r = k_.nodes[root_];
-        if (r.op == N_BLOCK) {
-            for (int s : kids_[root_]) statement(s);
-        } else {
-            statement(root_);
-        }
+        scheduleStatements();
         prog_.words.push_back(encode(OP_END, 0, 0, 0, 0));
         chainThroughAccumulator(prog_.words);
         prog_.registers = maxReg_;
@@ -152,6 +148,48 @@ private:
             if (loadUses_[key]++ == 0) loadOrder_.push_back(key);
         }
         for (int c : kids_[j]) collectLoads(c);
+    }
+
+    // Flattens nested BLOCKs into the statement list, in order.
+    void flatten(int j, std::vector<int>& out) const {
+        if (node(j).op == N_BLOCK) {
+            for (int c : kids_[j]) flatten(c, out);
+        } else {
+            out.push_back(j);
+        }
+    }
+
+    void localsRead(int j, std::vector<int>& out) const {
+        const symgb_node& nd = node(j);
+        if (nd.op == N_VAR && nd.b == G_LOCAL && std::find(out.begin(), out.end(), nd.a) == out.end()) out.push_back(nd.a);
+        for (int c : kids_[j]) localsRead(c, out);
+    }
+
+    // Emits statements in demand order: every output assignment in template
+    // order, each preceded by the definitions it still needs (depth first).
+    // This keeps definitions close to their uses, so fewer values are live
+    // at once.  Statements only assign distinct outputs or locals, so their
+    // order does not change any value.  Definitions no output needs are dropped.
+    void scheduleStatements() {
+        std::vector<int> stmts;
+        flatten(root_, stmts);
+        std::unordered_map<int, int> defOf;  // local id -> statement
+        for (int st : stmts)
+            if (node(st).op == N_DEFINE) defOf[node(kids_[st][0]).a] = st;
+        std::unordered_map<int, char> emitted;
+        std::function<void(int)> emit = [&](int st) {
+            if (emitted[st]) return;
+            emitted[st] = 1;
+            std::vector<int> needs;
+            localsRead(kids_[st][1], needs);
+            for (int l : needs) {
+                auto it = defOf.find(l);
+                if (it != defOf.end()) emit(it->second);
+            }
+            statement(st);
+        };
+        for (int st : stmts)
+            if (node(st).op != N_DEFINE) emit(st);
     }
 
     void countLocalUses(int j) {

@@ -90,7 +90,15 @@ ComputeKernel::ComputeKernel(const std::vector<Symbolic>& instances, int simdWid
         }
         const OpType parentOp = cur.op();
         const unsigned childPos = cur.childCounter;  // 1-based position of this child
+        // Every instance must have the same operation and child count here
+        // (the reference asserts this, ComputeKernel.cpp:166).
+        for (const Symbolic* xi : cur.x)
+            if (xi->op() != parentOp || xi->numChilds() != cur.numChilds())
+                throw GroupMismatch("kernel group holds structurally different blocks");
         Lockstep data(cur.x, childPos - 1);
+        if (data.op() == VAR || data.op() == CONST)  // leaf lists are never visited as `cur`
+            for (const Symbolic* xi : data.x)
+                if (xi->op() != data.op()) throw GroupMismatch("kernel group holds structurally different blocks");
         auto it = seen.find(data.h);
         if (it != seen.end()) {
             built.push_back(it->second);

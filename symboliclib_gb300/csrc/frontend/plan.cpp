@@ -13,6 +13,26 @@
 
 namespace symgb {
 
+namespace {
+
+// Structure fingerprint with non-linear mixing (operation, child count and
+// child fingerprints, leaves by kind only).  Used only to split a kernel group
+// whose blocks collide on the reference's CRC-based structure hash, which is
+// linear over GF(2) and so has systematic collisions.
+std::uint64_t structureFingerprint(const Symbolic& x) {
+    return traverseGenerateIdentity<std::uint64_t>(x, [](const Symbolic& y, const std::vector<std::uint64_t>& cs) {
+        std::uint64_t h = 0x9e3779b97f4a7c15ULL * (std::uint64_t)(y.op() + 1) + cs.size();
+        for (std::uint64_t c : cs) {
+            h ^= c + 0x9e3779b97f4a7c15ULL + (h << 6) + (h >> 2);
+            h *= 0xbf58476d1ce4e5b9ULL;
+            h ^= h >> 31;
+        }
+        return h;
+    });
+}
+
+}  // namespace
+
 // A container whose entries are all variables is an input: they must be
 // VAR(0..len-1, g) of one group g.  Any other container holds outputs, each
 // wrapped as ASSIGN(VAR(i, -10 - k), expr) for the k-th output container
@@ -61,23 +81,41 @@ Plan PlanBuilder::build() {
             id = (int)groups.size();
         }
     }
+    // A group whose blocks turn out to differ in structure (where the reference
+    // aborts) is split by structure fingerprint, in first-seen order;
+    // groups of identical blocks - every case the reference handles - are
+    // built exactly as the reference builds them.
     std::vector<int> blockGroup(blocks.size());
     std::vector<ComputeKernel> kernels;
     kernels.reserve(groups.size());
-    for (int g = 0; g < (int)groups.size(); ++g) {
+    auto widthFor = [&](std::size_t count) {
+        if (dev.vectorWidth == 0) return 0;
+        return count > dev.vectorWidth ? (int)dev.vectorWidth : 1;
+    };
+    for (std::size_t g = 0; g < groups.size(); ++g) {
         std::vector<Symbolic> inst(groups[g].size());
-        for (std::size_t j = 0; j < groups[g].size(); ++j) {
-            inst[j] = blocks[groups[g][j]].x;
-            blockGroup[groups[g][j]] = g;
+        for (std::size_t j = 0; j < groups[g].size(); ++j) inst[j] = blocks[groups[g][j]].x;
+        try {
+            kernels.emplace_back(inst, widthFor(inst.size()));
+            for (int b : groups[g]) blockGroup[b] = (int)kernels.size() - 1;
+        } catch (const GroupMismatch&) {
+            std::vector<std::vector<int>> parts;
+            std::unordered_map<std::uint64_t, int> partOf;
+            for (int b : groups[g]) {
+                int& p = partOf[structureFingerprint(blocks[b].x)];
+                if (!p) {
+                    parts.push_back({});
+                    p = (int)parts.size();
+                }
+                parts[p - 1].push_back(b);
+            }
+            for (auto& part : parts) {
+                std::vector<Symbolic> pi;
+                for (int b : part) pi.push_back(blocks[b].x);
+                kernels.emplace_back(pi, widthFor(pi.size()));
+                for (int b : part) blockGroup[b] = (int)kernels.size() - 1;
+            }
         }
-        int width;
-        if (dev.vectorWidth == 0)
-            width = 0;
-        else if (inst.size() > dev.vectorWidth)
-            width = (int)dev.vectorWidth;
-        else
-            width = 1;
-        kernels.emplace_back(inst, width);
     }
 
     // Execution order: children before parents (ComputeUnit.cpp:279-296).

@@ -13,6 +13,7 @@
 #include <array>
 #include <cmath>
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <tuple>
 #include <utility>
@@ -746,6 +747,82 @@ inline std::vector<std::tuple<int, int, double>> neoHookeanHessianUpper(const Te
                             for (int q = 0; q < 3; ++q) h += G[v][c] * G[w][q] * HF[3 * d + c][3 * e + q];
                         out.emplace_back(gi, gj, m.volume[t] * h);
                     }
+    }
+    return out;
+}
+
+// ---------------------------------------------------------------- random expression workloads
+
+// Random expression DAGs for training the schedule cost model.  `nShared`
+// random sub-expressions over the inputs are shared by the outputs (they
+// become intermediate blocks and dependency levels); each output applies one
+// of a few random template shapes to random inputs and shared values.  Shapes
+// mix sums, products, quotients and square roots of well-conditioned operands.
+template <class NT>
+struct RandomShape {
+    // post-order op list: 0 leaf, 1 add, 2 sub, 3 mul, 4 div, 5 sqrt-of-sum-of-squares
+    std::vector<int> ops;
+};
+
+inline RandomShape<double> randomShape(Rng& rng, int depth) {
+    RandomShape<double> s;
+    std::function<void(int)> gen = [&](int d) {
+        if (d == 0 || (d < depth && rng.uniform() < 0.25)) {  // the root is always an operation
+            s.ops.push_back(0);
+            return;
+        }
+        const int op = 1 + (int)rng.below(5);
+        gen(d - 1);
+        gen(d - 1);
+        s.ops.push_back(op);
+    };
+    gen(depth);
+    return s;
+}
+
+template <class NT, class Leaf>
+NT applyShape(const RandomShape<double>& s, Leaf&& leaf) {
+    std::vector<NT> st;
+    for (int op : s.ops) {
+        if (op == 0) {
+            st.push_back(leaf());
+            continue;
+        }
+        NT b = st.back();
+        st.pop_back();
+        NT a = st.back();
+        st.pop_back();
+        using std::sqrt;
+        switch (op) {
+            case 1: st.push_back(a + b); break;
+            case 2: st.push_back(a - b); break;
+            case 3: st.push_back(a * b); break;
+            case 4: st.push_back(a / (b * b + NT(1.0))); break;
+            default: st.push_back(sqrt(a * a + b * b + NT(1.0))); break;
+        }
+    }
+    return st.back();
+}
+
+template <class NT>
+std::vector<NT> randomExpressions(const std::vector<NT>& in, int outputs, std::uint64_t seed) {
+    Rng rng(seed);
+    const int nShapes = 1 + (int)rng.below(4), nShared = (int)rng.below(3) * (outputs / 8 + 1);
+    std::vector<RandomShape<double>> shapes;
+    for (int k = 0; k < nShapes; ++k) shapes.push_back(randomShape(rng, 2 + (int)rng.below(4)));
+    const RandomShape<double> sharedShape = randomShape(rng, 2 + (int)rng.below(3));
+    const int m = (int)in.size();
+    std::vector<NT> shared;
+    for (int k = 0; k < nShared; ++k)
+        shared.push_back(applyShape<NT>(sharedShape, [&]() { return in[rng.below((std::uint64_t)m)]; }));
+    std::vector<NT> out;
+    out.reserve(outputs);
+    for (int o = 0; o < outputs; ++o) {
+        const auto& sh = shapes[rng.below((std::uint64_t)nShapes)];
+        out.push_back(applyShape<NT>(sh, [&]() {
+            if (!shared.empty() && rng.uniform() < 0.3) return shared[rng.below(shared.size())];
+            return in[rng.below((std::uint64_t)m)];
+        }));
     }
     return out;
 }

@@ -99,6 +99,18 @@ int symgbw_build(const char* name, int size, unsigned long long seed, int vector
             w->inputs.push_back(vel);
             w->numeric = clothMatrix(r, X, vel, NoFix()).values;
             w->outputs = A.nnz();
+        } else if (n == "random") {
+            Rng rng(seed ^ 0x5eedULL);
+            const int m = std::max(8, size / 2);
+            std::vector<double> vals(m);
+            for (auto& v : vals) v = rng.uniform(0.5, 1.5);
+            auto VS = variables(vals.size(), 0);
+            auto out = randomExpressions(VS, size, seed);
+            pb.addContainer(VS.data(), VS.size());
+            pb.addContainer(out.data(), out.size());
+            w->inputs.push_back(vals);
+            w->numeric = randomExpressions(vals, size, seed);
+            w->outputs = out.size();
         } else if (n == "neohookean") {
             TetMesh m = tetMesh(size);
             std::vector<double> X = tetState(m, seed);

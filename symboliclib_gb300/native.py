@@ -37,7 +37,7 @@ class PlanDesc(C.Structure):
 class Schedule(C.Structure):
     _fields_ = [("kind", C.c_int32), ("math", C.c_int32), ("threads_per_block", C.c_int32),
                 ("items_per_tile", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32),
-                ("items_per_thread", C.c_int32)]
+                ("items_per_thread", C.c_int32), ("fusion_depth", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -74,6 +74,20 @@ SYMGB_FUNCTIONS = {
     "symgb_run_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p]),
     "symgb_measure_fp64_rate": (C.c_int, [C.POINTER(C.c_double)]),
+    "symgb_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "symgb_batch_run": (C.c_int, [C.c_void_p]),
+    "symgb_batch_run_async": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "symgb_batch_launch_count": (C.c_int, [C.c_void_p]),
+    "symgb_batch_destroy": (None, [C.c_void_p]),
+    "symgb_mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
+    "symgb_mlp_num_params": (C.c_int, [C.c_void_p]),
+    "symgb_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "symgb_mlp_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "symgb_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "symgb_mlp_gradient": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_float)]),
+    "symgb_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_float,
+                                  C.POINTER(C.c_float)]),
+    "symgb_mlp_destroy": (None, [C.c_void_p]),
     "symgb_kernel_program": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]),
 }
@@ -211,8 +225,9 @@ class Unit:
         return cls(w.plan, w.index_data, w.out_index_data, w.const_data)
 
     def set_schedule(self, kind=SCHEDULE_PLAIN, math=MATH_FAST, threads_per_block=0, items_per_tile=0,
-                     blocks_per_sm=0, use_graph=0, items_per_thread=1) -> None:
-        s = Schedule(kind, math, threads_per_block, items_per_tile, blocks_per_sm, use_graph, items_per_thread)
+                     blocks_per_sm=0, use_graph=0, items_per_thread=1, fusion_depth=0) -> None:
+        s = Schedule(kind, math, threads_per_block, items_per_tile, blocks_per_sm, use_graph, items_per_thread,
+                     fusion_depth)
         check(self._lib.symgb_set_schedule(self.handle, C.byref(s)))
 
     def set_num_sets(self, n: int) -> None:
@@ -250,6 +265,63 @@ class Unit:
     def close(self) -> None:
         if self.handle:
             self._lib.symgb_unit_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MLP:
+    """The engine's FP32 cost-model network (include/symgb.h, symgb_mlp_*)."""
+
+    def __init__(self, inputs: int, hidden: int = 64, seed: int = 0):
+        self._lib = symgb()
+        h = C.c_void_p()
+        check(self._lib.symgb_mlp_create(inputs, hidden, seed, C.byref(h)))
+        self.handle, self.inputs, self.hidden = h, inputs, hidden
+
+    @property
+    def num_params(self) -> int:
+        return self._lib.symgb_mlp_num_params(self.handle)
+
+    def params(self) -> np.ndarray:
+        p = np.empty(self.num_params, np.float32)
+        check(self._lib.symgb_mlp_get_params(self.handle, p.ctypes.data))
+        return p
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        check(self._lib.symgb_mlp_set_params(self.handle, p.ctypes.data))
+
+    def predict(self, X: np.ndarray) -> np.ndarray:
+        X = np.ascontiguousarray(X, np.float32)
+        y = np.empty(len(X), np.float32)
+        check(self._lib.symgb_mlp_forward(self.handle, X.ctypes.data, len(X), y.ctypes.data))
+        return y
+
+    def gradient(self, X: np.ndarray, y: np.ndarray) -> tuple[np.ndarray, float]:
+        X = np.ascontiguousarray(X, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        g = np.empty(self.num_params, np.float32)
+        loss = C.c_float()
+        check(self._lib.symgb_mlp_gradient(self.handle, X.ctypes.data, y.ctypes.data, len(X), g.ctypes.data,
+                                           C.byref(loss)))
+        return g, loss.value
+
+    def train(self, X: np.ndarray, y: np.ndarray, epochs: int, lr: float = 1e-3) -> float:
+        X = np.ascontiguousarray(X, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        loss = C.c_float()
+        check(self._lib.symgb_mlp_train(self.handle, X.ctypes.data, y.ctypes.data, len(X), epochs, lr,
+                                        C.byref(loss)))
+        return loss.value
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.symgb_mlp_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

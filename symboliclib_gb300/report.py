@@ -1,0 +1,247 @@
+"""Measurements of the engine on the workloads beyond the headline benchmark.
+
+    python -m symboliclib_gb300.report single --workload cloth --size 300 --sets 64
+        plain per-call path (one value set, one launch per kernel, the
+        reference's structure) against the batched, tuned engine on the same
+        workload; nonzeros/s, algorithmic HBM GB/s and FP64 fraction.
+    python -m symboliclib_gb300.report batch --count 64 --min-side 8 --max-side 48
+        many cloth patterns of uneven size, 1-16 value sets each, evaluated by
+        one CUDA-graph replay, against per-call plain evaluation of every set.
+    python -m symboliclib_gb300.report learned --target neohookean --target-size 6
+        the MLP cost model trained on tuner timings of other workloads, then
+        used to pick the target's schedule: regret and tuning time against
+        exhaustive search.
+Each prints one JSON line.  Errors are measured against the workload's FP64
+model evaluated in double (floor 1e-4 of the largest magnitude).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import native, tuner
+
+PEAKS = Path(__file__).resolve().parent.parent / "MEASURED_PEAKS.json"
+
+
+def hbm_peak():
+    try:
+        return float(json.loads(PEAKS.read_text())["hbm_gbs"])
+    except Exception:
+        return 6800.0
+
+
+def rel_err(a, ref, floor_frac=1e-4):
+    floor = floor_frac * np.max(np.abs(ref))
+    return float(np.max(np.abs(a - ref) / np.maximum(np.abs(ref), floor)))
+
+
+def flush_buffer():
+    import torch
+    return torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+
+
+def fp64_peak():
+    v = C.c_double()
+    native.check(native.symgb().symgb_measure_fp64_rate(C.byref(v)))
+    return v.value
+
+
+def single(args):
+    t0 = time.perf_counter()
+    w = native.Workload(args.workload, args.size, args.seed)
+    front = time.perf_counter() - t0
+    nnz = len(w.numeric)
+    u = native.Unit.from_workload(w)
+    stream = tuner.bind_stream(u)
+    flush = flush_buffer()
+    # plain per-call path: one value set, one launch per kernel
+    for i, a in enumerate(w.inputs):
+        u.set_arg(i, a)
+    plain = tuner.Sched("plain", 1, 128, 1)
+    plain.apply(u, graph=0)
+    u.run()
+    err_plain = rel_err(u.get_result(0), w.numeric)
+    t_plain = tuner.time_schedule(u, plain, stream, flush, runs=args.steps) * 1e-6
+    # batched value sets, tuned
+    S = args.sets
+    u.set_num_sets(S)
+    for i, a in enumerate(w.inputs):
+        u.set_arg(i, np.tile(a, S))
+    space = tuner.SPACE if args.full_space else [s for s in tuner.SPACE if s.tile == 1]
+    tt = time.perf_counter()
+    res = tuner.exhaustive(u, stream, flush, space=space, runs=max(3, args.steps // 2))
+    tune_s = time.perf_counter() - tt
+    t_batch = tuner.time_schedule(u, res.best, stream, flush, runs=args.steps) * 1e-6
+    res.best.apply(u)
+    u.run()
+    out = u.get_result(0).reshape(S, -1)
+    err_batch = max(rel_err(out[s], w.numeric) for s in (0, S - 1))
+    st = u.stats()
+    alg = u.algorithmic_bytes(S)
+    peak = hbm_peak()
+    fp = fp64_peak()
+    flops = (st.flops + 10 * st.divs + 10 * st.sqrts) * S
+    print(json.dumps({
+        "workload": f"{args.workload} {args.size}", "output_nnz": nnz, "value_sets": S, "front_end_s": round(front, 1),
+        "kernels": int(st.num_kernels), "levels": int(st.num_levels), "max_registers": int(st.max_registers),
+        "plain": {"ms_per_execute": t_plain * 1e3, "nnz_per_s": nnz / t_plain, "max_rel_err": err_plain,
+                  "hbm_gbs": u.algorithmic_bytes(1) / t_plain / 1e9},
+        "batched": {"schedule": str(res.best), "ms_per_execute": t_batch * 1e3, "nnz_per_s": nnz * S / t_batch,
+                    "max_rel_err": err_batch, "algorithmic_bytes": alg, "hbm_gbs": alg / t_batch / 1e9,
+                    "hbm_frac": alg / t_batch / 1e9 / peak, "fp64_tflops": flops / t_batch / 1e12,
+                    "fp64_frac": flops / t_batch / fp, "tuning_s": round(tune_s, 1), "schedules_timed": res.timed},
+        "speedup_batched_vs_plain": (nnz * S / t_batch) / (nnz / t_plain),
+        "hbm_peak_gbs": peak, "fp64_peak_tflops": fp / 1e12}), flush=True)
+
+
+def batch(args):
+    import torch
+    lib = native.symgb()
+    rng = np.random.default_rng(args.seed)
+    sides = np.exp(rng.uniform(math.log(args.min_side), math.log(args.max_side), args.count)).round().astype(int)
+    sets = rng.integers(1, args.max_sets + 1, args.count)
+    cache = {}
+    t0 = time.perf_counter()
+    units, total_nnz, plain_s = [], 0, 0.0
+    flush = flush_buffer()
+    for k, (side, S) in enumerate(zip(sides, sets)):
+        if side not in cache:
+            cache[side] = native.Workload("cloth", int(side), args.seed + int(side))
+        w = cache[side]
+        u = native.Unit.from_workload(w)
+        units.append((u, int(S), w))
+        total_nnz += len(w.numeric) * int(S)
+    front = time.perf_counter() - t0
+    # per-call plain evaluation of every value set (time of one set x S)
+    stream = torch.cuda.Stream()
+    plain_by_side = {}
+    for u, S, w in units:
+        native.check(lib.symgb_set_stream(u.handle, C.c_void_p(stream.cuda_stream)))
+        key = w.size
+        if key not in plain_by_side:
+            for i, a in enumerate(w.inputs):
+                u.set_arg(i, a)
+            plain_by_side[key] = tuner.time_schedule(u, tuner.Sched("plain", 1, 128, 1), stream, None, runs=5) * 1e-6
+        plain_s += plain_by_side[key] * S
+    # batched: each unit with its sets, tuned schedule choice per unit size class, one graph
+    for u, S, w in units:
+        u.set_num_sets(S)
+        for i, a in enumerate(w.inputs):
+            u.set_arg(i, np.tile(a, S))
+        tuner.Sched(args.schedule, 1, 128, 1).apply(u, graph=0)
+    handles = (C.c_void_p * len(units))(*[u.handle.value for u, _, _ in units])
+    b = C.c_void_p()
+    native.check(lib.symgb_batch_create(handles, len(units), args.streams, C.byref(b)))
+    for _ in range(3):
+        native.check(lib.symgb_batch_run(b))
+    ts = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        native.check(lib.symgb_batch_run_async(b, C.c_void_p(stream.cuda_stream)))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    t_graph = float(np.median(ts))
+    errs = []
+    for u, S, w in units[:8]:
+        out = u.get_result(0).reshape(S, -1)
+        errs.append(rel_err(out[S - 1], w.numeric))
+    launches = lib.symgb_batch_launch_count(b)
+    lib.symgb_batch_destroy(b)
+    print(json.dumps({
+        "instances": int(args.count), "sides": [int(sides.min()), int(sides.max())], "distinct_patterns": len(cache),
+        "value_sets_total": int(sets.sum()), "output_nnz_total": int(total_nnz), "front_end_s": round(front, 1),
+        "graph": {"ms": t_graph * 1e3, "nnz_per_s": total_nnz / t_graph, "kernels": int(launches),
+                  "streams": args.streams, "schedule": args.schedule},
+        "plain_per_call": {"ms": plain_s * 1e3, "nnz_per_s": total_nnz / plain_s},
+        "speedup": plain_s / t_graph, "max_rel_err_sampled": max(errs)}), flush=True)
+
+
+def learned(args):
+    """Cost model trained on tuner timings of other workloads, applied to the target."""
+    train = [("cotan", s, 1 + s) for s in (60, 120, 200)] + [("cloth", s, 2 + s) for s in (12, 20, 30)] + \
+            [("ata", s, 3 + s) for s in (40, 70)] + [("random", n, 10 + k) for k, n in
+                                                      enumerate([20000, 40000, 60000, 90000] * 5)]
+    X, y = [], []
+    t_collect = time.perf_counter()
+    for spec in train:
+        w = native.Workload(*spec)
+        u = native.Unit.from_workload(w)
+        for i, a in enumerate(w.inputs):
+            u.set_arg(i, a)
+        stream = tuner.bind_stream(u)
+        for S in ((1, 8) if spec[0] in ("cloth", "cotan") else (1,)):
+            u.set_num_sets(S)
+            for i, a in enumerate(w.inputs):
+                u.set_arg(i, np.tile(a, S))
+            res = tuner.exhaustive(u, stream, runs=3)
+            st = u.stats()
+            for s, t in res.timings.items():
+                X.append(tuner.features(st, S, s))
+                y.append(t)
+    t_collect = time.perf_counter() - t_collect
+    model = tuner.CostModel(seed=args.seed)
+    t_fit = time.perf_counter()
+    loss = model.fit(np.stack(X), np.array(y), epochs=args.epochs)
+    t_fit = time.perf_counter() - t_fit
+    w = native.Workload(args.target, args.target_size, args.seed)
+    u = native.Unit.from_workload(w)
+    for i, a in enumerate(w.inputs):
+        u.set_arg(i, a)
+    stream = tuner.bind_stream(u)
+    flush = flush_buffer()
+    full = tuner.exhaustive(u, stream, flush, runs=5)
+    prop = tuner.tune_with_model(u, model, stream, flush, k=args.k, runs=5)
+    print(json.dumps({
+        "target": f"{args.target} {args.target_size}", "output_nnz": len(w.numeric),
+        "training_samples": len(y), "training_units": len(train), "collect_s": round(t_collect, 1),
+        "fit_s": round(t_fit, 2), "fit_mse_log": loss,
+        "exhaustive": {"best": str(full.best), "best_us": full.best_us, "timed": full.timed, "seconds": full.seconds},
+        "learned": {"best": str(prop.best), "best_us": full.timings.get(prop.best, prop.best_us), "timed": prop.timed,
+                    "seconds": prop.seconds},
+        "regret": full.timings.get(prop.best, prop.best_us) / full.best_us - 1.0,
+        "tuning_time_ratio": full.seconds / max(prop.seconds, 1e-9),
+        "timings_ratio": full.timed / max(1, prop.timed)}), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    a = sub.add_parser("single")
+    a.add_argument("--workload", default="cloth")
+    a.add_argument("--size", type=int, default=300)
+    a.add_argument("--sets", type=int, default=64)
+    a.add_argument("--seed", type=int, default=2024)
+    a.add_argument("--steps", type=int, default=10)
+    a.add_argument("--full-space", action="store_true")
+    b = sub.add_parser("batch")
+    b.add_argument("--count", type=int, default=64)
+    b.add_argument("--min-side", type=int, default=8)
+    b.add_argument("--max-side", type=int, default=48)
+    b.add_argument("--max-sets", type=int, default=16)
+    b.add_argument("--streams", type=int, default=8)
+    b.add_argument("--schedule", default="levels", choices=list(tuner.KINDS))
+    b.add_argument("--seed", type=int, default=7)
+    b.add_argument("--steps", type=int, default=10)
+    c = sub.add_parser("learned")
+    c.add_argument("--target", default="neohookean")
+    c.add_argument("--target-size", type=int, default=6)
+    c.add_argument("--k", type=int, default=3)
+    c.add_argument("--epochs", type=int, default=4000)
+    c.add_argument("--seed", type=int, default=5)
+    args = ap.parse_args()
+    {"single": single, "batch": batch, "learned": learned}[args.cmd](args)
+
+
+if __name__ == "__main__":
+    main()

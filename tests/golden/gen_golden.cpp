@@ -212,6 +212,14 @@ int main(int argc, char** argv) {
         std::vector<double> all(X);
         all.insert(all.end(), vel.begin(), vel.end());
         run(out, A.values, all, {X, vel}, {XS, VS});
+    } else if (w == "random") {
+        Rng rng(seed ^ 0x5eedULL);
+        const int m = std::max(8, size / 2);
+        std::vector<double> vals(m);
+        for (auto& v : vals) v = rng.uniform(0.5, 1.5);
+        auto VS = variables(vals.size(), 0);
+        auto outv = randomExpressions(VS, size, seed);
+        run(out, outv, vals, {vals}, {VS});
     } else if (w == "neohookean") {
         TetMesh m = tetMesh(size);
         std::vector<double> X = tetState(m, seed);

@@ -104,3 +104,23 @@ def test_vector_width_plan_shapes():
             assert n4 % 4 == 0 and n4 - n0 < 4
         else:
             assert n4 == n0
+
+
+@pytest.mark.parametrize("seed", [22, 28, 3, 7])
+def test_random_expression_plans_are_valid(seed):
+    """Random expression DAGs, including seeds whose blocks collide on the
+    reference's (GF(2)-linear) structure hash: the reference aborts on seed 22
+    (ComputeKernel.cpp:166) and builds out-of-range index tables on seed 28;
+    the engine splits such groups by structure, so every index stays inside x
+    and the plan evaluates to the FP64 model."""
+    w = native.Workload("random", 2000, seed)
+    d = w.plan.contents
+    for k in range(d.num_kernels):
+        kd = d.kernels[k]
+        n = kd.num_instances
+        for a in range(kd.num_access):
+            base, off = kd.access[2 * a], kd.access[2 * a + 1]
+            p = w.index_data[kd.index_offset + base * n: kd.index_offset + (base + 1) * n].astype(np.int64) + off
+            assert p.min() >= 0 and p.max() < d.num_total_memory
+    out = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
+    assert rel_err(out, w.numeric) <= 1e-12

@@ -1,0 +1,155 @@
+"""GPU tests of schedules beyond the basic three, multi-unit graph batches,
+the cost model's FP32 kernels (gradients against the CPU oracle) and the
+learned schedule proposer."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from symboliclib_gb300 import native, tuner
+
+import oracle.cpu as ocpu
+import oracle.mlp as omlp
+
+pytestmark = pytest.mark.gpu
+
+
+def bits_equal(a, b):
+    return a.shape == b.shape and np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def split_inputs(w, flat):
+    out, off = [], 0
+    for a in w.inputs:
+        out.append(flat[off:off + len(a)])
+        off += len(a)
+    return out
+
+
+@pytest.mark.parametrize("depth", [2, 3])
+@pytest.mark.parametrize("graph", [0, 1])
+def test_fusion_depth_and_graphs_bit_exact(depth, graph):
+    for name, size, seed in [("cotan", 8, 22), ("cloth", 5, 32), ("neohookean", 2, 42)]:
+        _, inp, gold = load_golden(name, size)
+        w = native.Workload(name, size, seed)
+        u = native.Unit.from_workload(w)
+        u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_EXACT, fusion_depth=depth, use_graph=graph)
+        for i, a in enumerate(split_inputs(w, inp)):
+            u.set_arg(i, a)
+        for _ in range(2):
+            u.run()
+            assert bits_equal(u.get_result(0), gold), (name, depth, graph)
+        u.set_schedule(kind=native.SCHEDULE_PERSISTENT, math=native.MATH_EXACT, use_graph=graph)
+        u.run()
+        assert bits_equal(u.get_result(0), gold), (name, "persistent", graph)
+
+
+def test_every_tuner_schedule_is_exact():
+    _, inp, gold = load_golden("cloth", 5)
+    w = native.Workload("cloth", 5, 32)
+    u = native.Unit.from_workload(w)
+    for i, a in enumerate(split_inputs(w, inp)):
+        u.set_arg(i, a)
+    for s in tuner.SPACE:
+        s.apply(u, native.MATH_EXACT)
+        u.run()
+        assert bits_equal(u.get_result(0), gold), s
+
+
+def test_batch_graph_matches_individual_runs():
+    """Units of uneven size and value-set count in one graph replay."""
+    lib = native.symgb()
+    units, refs = [], []
+    rng = np.random.default_rng(3)
+    for k, (name, size) in enumerate([("cloth", 4), ("cloth", 9), ("cotan", 30), ("cloth", 6), ("ata", 10)]):
+        w = native.Workload(name, size, 100 + k)
+        u = native.Unit.from_workload(w)
+        S = int(rng.integers(1, 17))
+        kind = [native.SCHEDULE_PLAIN, native.SCHEDULE_LEVELS, native.SCHEDULE_PERSISTENT][k % 3]
+        u.set_schedule(kind=kind, math=native.MATH_EXACT)
+        u.set_num_sets(S)
+        per_set = [[a * (1.0 + 0.01 * s) for a in w.inputs] for s in range(S)]
+        for i in range(len(w.inputs)):
+            u.set_arg(i, np.concatenate([ps[i] for ps in per_set]))
+        ref = [ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, per_set[s])[0] for s in (0, S - 1)]
+        units.append((w, u, S))
+        refs.append(ref)
+    handles = (C.c_void_p * len(units))(*[u.handle.value for _, u, _ in units])
+    b = C.c_void_p()
+    native.check(lib.symgb_batch_create(handles, len(units), 4, C.byref(b)))
+    try:
+        assert lib.symgb_batch_launch_count(b) >= len(units)
+        for _ in range(2):
+            native.check(lib.symgb_batch_run(b))
+            for (w, u, S), ref in zip(units, refs):
+                out = u.get_result(0).reshape(S, -1)
+                assert bits_equal(out[0], ref[0]) and bits_equal(out[S - 1], ref[1])
+    finally:
+        lib.symgb_batch_destroy(b)
+
+
+def test_mlp_gradient_matches_cpu_oracle():
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((300, 23)).astype(np.float32)
+    y = rng.standard_normal(300).astype(np.float32)
+    net = native.MLP(23, 64, seed=5)
+    g, loss = net.gradient(X, y)
+    g_ref, loss_ref = omlp.gradient(net.params(), X, y, 23, 64)
+    assert abs(loss - loss_ref) <= 1e-4 * max(1.0, loss_ref)
+    scale = np.max(np.abs(g_ref))
+    assert np.max(np.abs(g - g_ref)) <= 1e-4 * scale
+    pred = net.predict(X)
+    ref_pred, _ = omlp.forward(net.params(), X, 23, 64)
+    assert np.max(np.abs(pred - ref_pred)) <= 1e-4 * max(1.0, np.max(np.abs(ref_pred)))
+
+
+def test_mlp_training_fits_a_smooth_function():
+    rng = np.random.default_rng(1)
+    X = rng.uniform(-1, 1, (2000, 4)).astype(np.float32)
+    y = (np.sin(2 * X[:, 0]) + X[:, 1] * X[:, 2] - 0.5 * X[:, 3] ** 2).astype(np.float32)
+    net = native.MLP(4, 64, seed=2)
+    before = float(np.mean((net.predict(X) - y) ** 2))
+    after = net.train(X, y, epochs=2000, lr=3e-3)
+    assert after < 0.05 * before and after < 0.01
+
+
+def test_learned_proposer_beats_untrained_choice():
+    """What the trained network gains.  The cost model is trained on the
+    tuner's timings of one set of units and evaluated on held-out units.
+    Timing only its top-3 schedules costs 3 timings instead of len(SPACE)
+    (24x fewer) and must stay within 10% mean regret of exhaustive search, and
+    do better than the same budget spent without the network (3 schedules
+    drawn at random)."""
+    train_units = [("random", 60000, s) for s in range(10)] + [("cotan", 100, 1), ("cloth", 20, 2), ("ata", 60, 3)]
+    test_units = [("random", 90000, 100 + s) for s in range(6)] + [("cotan", 150, 7), ("cloth", 26, 8),
+                                                                    ("neohookean", 3, 9)]
+    X, y, held = [], [], []
+    for spec in train_units + test_units:
+        w = native.Workload(*spec)
+        u = native.Unit.from_workload(w)
+        for i, a in enumerate(w.inputs):
+            u.set_arg(i, a)
+        stream = tuner.bind_stream(u)
+        res = tuner.exhaustive(u, stream, runs=5)
+        st = u.stats()
+        if spec in train_units:
+            for s, t in res.timings.items():
+                X.append(tuner.features(st, 1, s))
+                y.append(t)
+        else:
+            held.append((res, st))
+    model = tuner.CostModel(seed=0)
+    model.fit(np.stack(X), np.array(y), epochs=3000)
+    rng = np.random.default_rng(4)
+    regret_model, regret_random = [], []
+    for res, st in held:
+        picks = tuner.propose(model, st, 1, k=3)
+        regret_model.append(min(res.timings[s] for s in picks if s in res.timings) / res.best_us - 1.0)
+        for _ in range(20):  # expected regret of 3 random picks
+            blind = [tuner.SPACE[i] for i in rng.choice(len(tuner.SPACE), 3, replace=False)]
+            regret_random.append(min(res.timings[s] for s in blind if s in res.timings) / res.best_us - 1.0)
+    print("mean regret: model top-3", np.mean(regret_model), "random 3", np.mean(regret_random))
+    assert len(tuner.SPACE) / 3 >= 10
+    assert np.mean(regret_model) <= 0.10
+    assert np.mean(regret_model) < np.mean(regret_random)

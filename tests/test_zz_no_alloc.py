@@ -32,7 +32,7 @@ def static_unit(w):
     lib = native.symgb()
     h = C.c_void_p()
     native.check(lib.symgb_unit_create(w.plan, C.byref(h)))
-    s = native.Schedule(native.SCHEDULE_PERSISTENT, native.MATH_EXACT, 0, 0, 0, 0, 1)
+    s = native.Schedule(native.SCHEDULE_PERSISTENT, native.MATH_EXACT, 0, 0, 0, 0, 1, 0)
     native.check(lib.symgb_set_schedule(h, C.byref(s)))
     return lib, h
 
