@@ -107,6 +107,9 @@ typedef struct symgb_schedule {
     int32_t items_per_thread;   /* work items per thread per pass: 1, 2 or 4 (0 = 1) */
     int32_t fusion_depth;       /* LEVELS: consecutive levels per launch (0/1 = one level; a
                                    group of several levels is one cooperative launch) */
+    int32_t lanes_per_item;     /* threads sharing one work item: 1, 2, 4 or 8 (0 = 1).  They
+                                   split every bundle of the program and share the item's
+                                   register file, which divides its shared memory per thread */
 } symgb_schedule;
 
 /* --- the reference's generated-library calls, per unit ----------------------- */
@@ -198,6 +201,8 @@ typedef struct symgb_stats {
     uint64_t gathers;         /* x reads per value set */
     uint64_t max_registers;   /* largest per-thread register file of a kernel program */
     uint64_t program_words;   /* total device program length (64-bit words) */
+    uint64_t bundles;         /* per value set: compute bundles dispatched (instances x bundles) */
+    uint64_t bundle_entries;  /* per value set: operations in those bundles */
 } symgb_stats;
 int symgb_get_stats(symgb_unit_t u, symgb_stats* s);
 
@@ -207,7 +212,7 @@ uint64_t symgb_algorithmic_bytes(symgb_unit_t u, int num_sets);
 
 /* Introspection: the device program of kernel k for a math mode (64-bit words
  * as executed by the interpreter kernels: the load section, then the compute
- * section).  Writes up to `cap` words, the register count and the length of
+ * bundles, an end word and the literal table).  Writes up to `cap` words, the register count and the length of
  * the load section; returns the program length in words, or a negative error. */
 int64_t symgb_kernel_program(symgb_unit_t u, int k, int math, uint64_t* words, uint64_t cap, int* registers,
                              int* num_loads);

@@ -46,7 +46,7 @@ ORACLE_SRC = [ROOT / "oracle" / "evaluate.c"]
 
 def _headers() -> list[Path]:
     return (list(INCLUDE.rglob("*.h")) + list(INCLUDE.rglob("*.hpp")) + list(CSRC.rglob("*.hpp"))
-            + [Path(__file__)])
+            + list(CSRC.rglob("*.cuh")) + [Path(__file__)])
 
 
 def _stale(target: Path, deps: list[Path]) -> bool:

@@ -21,8 +21,8 @@ struct DevKernel {
     std::uint64_t n;            // instances
     std::uint32_t regs;         // register-file slots used
     std::uint32_t nloads;       // words in the loads section
-    std::uint32_t nwords;       // total program words (loads + compute)
-    std::uint32_t pad;
+    std::uint32_t nwords;       // total program words (loads + compute + literals)
+    std::uint32_t litoff;       // first word of the literal table
 };
 
 struct Tile {
@@ -38,7 +38,11 @@ struct BarrierState {
     int pad;
 };
 
-enum : int { LOAD_CACHED = 0, LOAD_L2 = 1 };
+// Interpreter variants: MODE_L2 reads x through L2 only (x written earlier in
+// the same launch); MODE_LIB adds the library operations (pow, sin, ...),
+// whose code needs many registers, so programs without them run a variant
+// with a smaller register footprint and higher occupancy.
+enum : int { LOAD_CACHED = 0, LOAD_L2 = 1, MODE_L2 = 1, MODE_LIB = 2 };
 
 struct EvalArgs {
     const DevKernel* ks;
@@ -49,7 +53,7 @@ struct EvalArgs {
     double* xw;
     unsigned S;
     unsigned progCap;               // program words that fit in shared memory (0: read from global)
-    unsigned regStride;             // unused, reserved
+    unsigned lanes;                 // threads per work item (1, 2, 4 or 8)
     BarrierState* bar;
     int* hostError;
     unsigned long long timeoutNs;
@@ -68,10 +72,131 @@ __device__ __forceinline__ double loadX(const double* a) {
     return __ldg(a);
 }
 
-__device__ __forceinline__ double dfma(double a, double b, double c, int flags) {
-    if (flags & symgb::engine::FMA_NEG_PRODUCT) a = -a;
-    if (flags & symgb::engine::FMA_NEG_ADDEND) c = -c;
-    return __fma_rn(a, b, c);
+// Negation flips the sign bit (as C's unary minus does), on the integer pipe.
+__device__ __forceinline__ double negate(double x) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+
+struct AddOp {
+    __device__ double operator()(double x, double y, double) const { return __dadd_rn(x, y); }
+};
+struct SubOp {
+    __device__ double operator()(double x, double y, double) const { return __dsub_rn(x, y); }
+};
+struct MulOp {
+    __device__ double operator()(double x, double y, double) const { return __dmul_rn(x, y); }
+};
+struct DivOp {
+    __device__ double operator()(double x, double y, double) const { return __ddiv_rn(x, y); }
+};
+template <bool NEG_PRODUCT, bool NEG_ADDEND>
+struct FmaOp {  // (+-)(x * y) (+-) z, one rounding
+    __device__ double operator()(double x, double y, double z) const {
+        return __fma_rn(NEG_PRODUCT ? negate(x) : x, y, NEG_ADDEND ? negate(z) : z);
+    }
+};
+struct NegOp {
+    __device__ double operator()(double x, double, double) const { return negate(x); }
+};
+struct MovOp {
+    __device__ double operator()(double x, double, double) const { return x; }
+};
+struct SqrtOp {
+    __device__ double operator()(double x, double, double) const { return __dsqrt_rn(x); }
+};
+struct RecOp {
+    __device__ double operator()(double x, double, double) const { return __ddiv_rn(1.0, x); }
+};
+template <int OPC>
+struct LibOp {  // CUDA's double-precision math library
+    __device__ double operator()(double x, double y, double) const {
+        switch (OPC) {
+            case symgb::engine::OP_POW: return pow(x, y);
+            case symgb::engine::OP_SIN: return sin(x);
+            case symgb::engine::OP_COS: return cos(x);
+            case symgb::engine::OP_TAN: return tan(x);
+            case symgb::engine::OP_ASIN: return asin(x);
+            case symgb::engine::OP_ACOS: return acos(x);
+            case symgb::engine::OP_ATAN: return atan(x);
+            case symgb::engine::OP_EXP: return exp(x);
+            default: return log(x);
+        }
+    }
+};
+
+// Entries of a bundle processed together: their operand reads, operations and
+// result writes are issued as three batches, so GROUP operations (times the
+// items per thread) of one thread are in flight at once.
+constexpr unsigned GROUP = 4;
+constexpr unsigned LONG_GROUP = 2;  // division and square root: long sequences with many temporaries
+
+__device__ __forceinline__ unsigned field(std::uint32_t e, int f) { return (e >> (8 * f)) & 0xffu; }
+
+// Register file view of one thread: R[r * stride + j * T] is register r of item j.
+struct RegFile {
+    double* R;
+    unsigned stride, T;
+    __device__ __forceinline__ double& at(unsigned r, int j) const { return R[r * stride + j * T]; }
+};
+
+// Runs the entries lane, lane + P, lane + 2P, ... of a bundle (P = lanes per
+// work item; the other lanes of the item run the rest).
+// Single-entry bundles may take operands from, and leave their result only in,
+// the accumulator `acc` (header flags; see program.hpp).
+template <int ITEMS, int NSRC, unsigned GROUP, class F>
+__device__ __forceinline__ void runBundle(const std::uint32_t* e, unsigned cnt, const RegFile& rf, unsigned lane,
+                                          unsigned P, unsigned flags, double (&acc)[ITEMS], F f) {
+    unsigned q = lane;
+    for (; q + (GROUP - 1) * P < cnt; q += GROUP * P) {
+        std::uint32_t ee[GROUP];
+#pragma unroll
+        for (unsigned u = 0; u < GROUP; ++u) ee[u] = e[q + u * P];
+        double v[GROUP][NSRC][ITEMS];
+#pragma unroll
+        for (unsigned u = 0; u < GROUP; ++u)
+#pragma unroll
+            for (int s = 0; s < NSRC; ++s)
+#pragma unroll
+                for (int j = 0; j < ITEMS; ++j) v[u][s][j] = rf.at(field(ee[u], s + 1), j);
+        double r[GROUP][ITEMS];
+#pragma unroll
+        for (unsigned u = 0; u < GROUP; ++u)
+#pragma unroll
+            for (int j = 0; j < ITEMS; ++j) r[u][j] = f(v[u][0][j], v[u][NSRC > 1 ? 1 : 0][j], v[u][NSRC > 2 ? 2 : 0][j]);
+#pragma unroll
+        for (unsigned u = 0; u < GROUP; ++u)
+#pragma unroll
+            for (int j = 0; j < ITEMS; ++j) rf.at(field(ee[u], 0), j) = r[u][j];
+    }
+    for (; q < cnt; q += P) {
+        const std::uint32_t e0 = e[q];
+        double v[NSRC][ITEMS];
+#pragma unroll
+        for (int s = 0; s < NSRC; ++s)
+#pragma unroll
+            for (int j = 0; j < ITEMS; ++j) v[s][j] = (flags & (H_A_ACC << s)) ? acc[j] : rf.at(field(e0, s + 1), j);
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            acc[j] = f(v[0][j], v[NSRC > 1 ? 1 : 0][j], v[NSRC > 2 ? 2 : 0][j]);
+            if (!(flags & H_NOSTORE)) rf.at(field(e0, 0), j) = acc[j];
+        }
+    }
+}
+
+// One entry at a time (long library sequences: keeps the code small).  Not a
+// call: a call makes every live register of the caller survive it.
+template <int ITEMS, int NSRC, class F>
+__device__ __forceinline__ void runBundleSerial(const std::uint32_t* e, unsigned cnt, const RegFile& rf, unsigned lane,
+                                                unsigned P, F f) {
+    for (unsigned q = lane; q < cnt; q += P) {
+        const std::uint32_t e0 = e[q];
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            const double x = rf.at(field(e0, 1), j);
+            const double y = NSRC > 1 ? rf.at(field(e0, 2), j) : 0.0;
+            rf.at(field(e0, 0), j) = f(x, y, 0.0);
+        }
+    }
 }
 
 __device__ __forceinline__ unsigned long long globalTimerNs() {
@@ -116,161 +241,167 @@ __device__ bool gridBarrier(BarrierState* bar, int* hostError, unsigned long lon
 }
 
 
-// Evaluates one tile: ITEMS work items per thread.  Shared memory holds the
-// program (when it fits) followed by the register file, laid out
-// [register][item][thread] so a warp's accesses are conflict-free.
-template <int ITEMS, int LOAD>
+// Evaluates one tile.  A work item (one instance for one value set) is run by
+// P = A.lanes threads of one warp: warp lane l serves item slot l % (32 / P)
+// of its warp as lane l / (32 / P), so each half-warp touches consecutive
+// slots.  Each thread serves ITEMS item slots per pass.  Shared memory holds
+// the program (when it fits) followed by the register file, laid out
+// [register][item][slot] so a warp's accesses are conflict-free.  The lanes of
+// an item split every bundle; a warp barrier after each bundle makes their
+// results visible to each other.
+template <int ITEMS, int MODE>
 __device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t* prog, double* regs, const Tile& t,
                                          const EvalArgs& A) {
     using namespace symgb::engine;
-    const unsigned T = blockDim.x;
+    const unsigned P = A.lanes;
+    const unsigned perWarp = 32u / P;
+    const unsigned lane = (threadIdx.x & 31u) / perWarp;
+    const unsigned T = blockDim.x / P;  // item slots per block
+    const unsigned me = (threadIdx.x >> 5) * perWarp + (threadIdx.x & (perWarp - 1));
     const unsigned S = A.S;
+    const RegFile rf{regs + me, (unsigned)ITEMS * T, T};
+    const double* lit = reinterpret_cast<const double*>(prog + k.litoff);
     for (std::uint64_t base = 0; base < t.count; base += (std::uint64_t)T * ITEMS) {
         std::uint64_t ii[ITEMS];
         unsigned ss[ITEMS];
         bool valid[ITEMS];
 #pragma unroll
         for (int j = 0; j < ITEMS; ++j) {
-            std::uint64_t off = base + (std::uint64_t)j * T + threadIdx.x;
+            std::uint64_t off = base + (std::uint64_t)j * T + me;
             valid[j] = off < t.count;
             if (!valid[j]) off = t.count - 1;  // duplicate the last item; its stores are skipped
             const std::uint64_t w = t.start + off;
-            ii[j] = w / S;
-            ss[j] = (unsigned)(w - ii[j] * S);
+            if (S == 1) {
+                ii[j] = w;
+                ss[j] = 0;
+            } else if (w < 0xffffffffull) {
+                ii[j] = (std::uint32_t)w / S;
+                ss[j] = (unsigned)w - (unsigned)ii[j] * S;
+            } else {
+                ii[j] = w / S;
+                ss[j] = (unsigned)(w - ii[j] * S);
+            }
         }
-#define REG(r, j) regs[((unsigned)(r) * ITEMS + (j)) * T + threadIdx.x]
         // Loads: up to 8 entries at a time, all index loads, then all gathers.
+        // x slots fit in 32 bits (checked when the unit is created).
         const unsigned nl = k.nloads;
-        for (unsigned b = 0; b < nl; b += 8) {
-            std::uint64_t wv[8];
+        for (unsigned b = lane; b < nl; b += 8 * P) {
+            unsigned meta[8];
+            unsigned slot[8][ITEMS];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) wv[u] = (b + u < nl) ? prog[b + u] : 0ull;
-            long long idx[8][ITEMS];
+            for (int u = 0; u < 8; ++u) {
+                const std::uint64_t w = (b + u * P < nl) ? prog[b + u * P] : 0ull;
+                meta[u] = (unsigned)w & 0xffffu;  // op, destination register
+                const unsigned op = (unsigned)w & 0xffu;
+                const unsigned imm = (unsigned)(w >> 32);
 #pragma unroll
-            for (int u = 0; u < 8; ++u)
-#pragma unroll
-                for (int j = 0; j < ITEMS; ++j) {
-                    idx[u][j] = 0;
-                    if ((wv[u] & 0xff) == OP_LDX) {
-                        const unsigned row = (unsigned)(wv[u] >> 16) & 0xffff;
-                        idx[u][j] = (long long)__ldg(k.p + row * k.n + ii[j]) + (int)(unsigned)(wv[u] >> 32);
-                    }
-                }
+                for (int j = 0; j < ITEMS; ++j)
+                    slot[u][j] = op == OP_LDX ? __ldg(k.p + ((unsigned)(w >> 16) & 0xffffu) * k.n + ii[j]) + imm : imm;
+            }
             double v[8][ITEMS];
 #pragma unroll
             for (int u = 0; u < 8; ++u)
 #pragma unroll
                 for (int j = 0; j < ITEMS; ++j) {
-                    const unsigned op = (unsigned)(wv[u] & 0xff);
+                    const unsigned op = meta[u] & 0xffu;
                     if (op == OP_LDX)
-                        v[u][j] = loadX<LOAD>(A.x + (std::uint64_t)idx[u][j] * S + ss[j]);
+                        v[u][j] = loadX<MODE & MODE_L2>(A.x + (std::uint64_t)slot[u][j] * S + ss[j]);
                     else if (op == OP_LDC)
-                        v[u][j] = __ldg(k.c + (std::uint64_t)(unsigned)(wv[u] >> 32) * k.n + ii[j]);
+                        v[u][j] = __ldg(k.c + (std::uint64_t)slot[u][j] * k.n + ii[j]);
                     else
                         v[u][j] = 0.0;
                 }
 #pragma unroll
             for (int u = 0; u < 8; ++u)
-                if (b + u < nl) {
-                    const unsigned d = (unsigned)(wv[u] >> 8) & 0xff;
+                if (b + u * P < nl) {
 #pragma unroll
-                    for (int j = 0; j < ITEMS; ++j) REG(d, j) = v[u][j];
+                    for (int j = 0; j < ITEMS; ++j) rf.at(meta[u] >> 8, j) = v[u][j];
                 }
         }
-        // Arithmetic and stores.  `acc` holds the last result (per item); flag
-        // bits route single-use values through it instead of shared memory.
+        if (P > 1) __syncwarp();
+        // Compute bundles.
         double acc[ITEMS];
 #pragma unroll
         for (int j = 0; j < ITEMS; ++j) acc[j] = 0.0;
         for (const std::uint64_t* ip = prog + nl;;) {
-            const std::uint64_t w = *ip++;
-            const unsigned op = (unsigned)(w & 0xff);
-            const unsigned d = (unsigned)(w >> 8) & 0xff;
-            const unsigned a = (unsigned)(w >> 16) & 0xff;
-            const unsigned bb = (unsigned)(w >> 24) & 0xff;
-            const bool aAcc = (w & F_A_ACC) != 0, bAcc = (w & F_B_ACC) != 0, keep = (w & F_NOSTORE) == 0;
+            const std::uint64_t h = *ip;
+            const unsigned op = (unsigned)h & 0xffu;
             if (op == OP_END) break;
-#define OPA(j) (aAcc ? acc[j] : REG(a, j))
-#define OPB(j) (bAcc ? acc[j] : REG(bb, j))
-#define RESULT(j, v)              \
-    {                             \
-        const double r_ = (v);    \
-        acc[j] = r_;              \
-        if (keep) REG(d, j) = r_; \
-    }
+            const unsigned cnt = (unsigned)(h >> 8) & 0xffffu;
+            const unsigned flags = (unsigned)h & 0xff000000u;
+            const std::uint32_t* e = reinterpret_cast<const std::uint32_t*>(ip + 1);
+            ip += 1 + ((cnt + 1) >> 1);
             switch (op) {
-                case OP_LDK: {
-                    const double cv = __longlong_as_double((long long)*ip++);
+                case OP_ADD: runBundle<ITEMS, 2, GROUP>(e, cnt, rf, lane, P, flags, acc, AddOp{}); break;
+                case OP_SUB: runBundle<ITEMS, 2, GROUP>(e, cnt, rf, lane, P, flags, acc, SubOp{}); break;
+                case OP_MUL: runBundle<ITEMS, 2, GROUP>(e, cnt, rf, lane, P, flags, acc, MulOp{}); break;
+                case OP_DIV: runBundle<ITEMS, 2, LONG_GROUP>(e, cnt, rf, lane, P, flags, acc, DivOp{}); break;
+                case OP_FMA: runBundle<ITEMS, 3, GROUP>(e, cnt, rf, lane, P, flags, acc, FmaOp<false, false>{}); break;
+                case OP_FMS: runBundle<ITEMS, 3, GROUP>(e, cnt, rf, lane, P, flags, acc, FmaOp<false, true>{}); break;
+                case OP_FNMA: runBundle<ITEMS, 3, GROUP>(e, cnt, rf, lane, P, flags, acc, FmaOp<true, false>{}); break;
+                case OP_FNMS: runBundle<ITEMS, 3, GROUP>(e, cnt, rf, lane, P, flags, acc, FmaOp<true, true>{}); break;
+                case OP_NEG: runBundle<ITEMS, 1, GROUP>(e, cnt, rf, lane, P, flags, acc, NegOp{}); break;
+                case OP_MOV: runBundle<ITEMS, 1, GROUP>(e, cnt, rf, lane, P, flags, acc, MovOp{}); break;
+                case OP_SQRT: runBundle<ITEMS, 1, LONG_GROUP>(e, cnt, rf, lane, P, flags, acc, SqrtOp{}); break;
+                case OP_REC: runBundle<ITEMS, 1, LONG_GROUP>(e, cnt, rf, lane, P, flags, acc, RecOp{}); break;
+                case OP_POW: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 2>(e, cnt, rf, lane, P, LibOp<OP_POW>{}); break;
+                case OP_SIN: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_SIN>{}); break;
+                case OP_COS: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_COS>{}); break;
+                case OP_TAN: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_TAN>{}); break;
+                case OP_ASIN: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_ASIN>{}); break;
+                case OP_ACOS: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_ACOS>{}); break;
+                case OP_ATAN: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_ATAN>{}); break;
+                case OP_EXP: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_EXP>{}); break;
+                case OP_LOG: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_LOG>{}); break;
+                case OP_LDK:
+                    for (unsigned q = lane; q < cnt; q += P) {
+                        const std::uint32_t e0 = e[q];
+                        const double c = lit[e0 >> 8];
 #pragma unroll
-                    for (int j = 0; j < ITEMS; ++j) RESULT(j, cv)
+                        for (int j = 0; j < ITEMS; ++j) {
+                            acc[j] = c;
+                            if (!(flags & H_NOSTORE)) rf.at(field(e0, 0), j) = c;
+                        }
+                    }
                     break;
-                }
                 case OP_ST: {
-                    const std::uint64_t row = (std::uint64_t)((w >> 32) & 0xffffff);
+                    const std::uint64_t yoff = k.yoff, n = k.n;
+                    unsigned q = lane;
+                    for (; q + (GROUP - 1) * P < cnt; q += GROUP * P) {
+                        std::uint32_t ee[GROUP];
+                        double v[GROUP][ITEMS];
 #pragma unroll
-                    for (int j = 0; j < ITEMS; ++j)
-                        if (valid[j]) A.xw[(k.yoff + row * k.n + ii[j]) * S + ss[j]] = OPA(j);
-                    break;
-                }
-#define BIN(OPC, EXPR)                                                 \
-    case OPC: {                                                        \
-        _Pragma("unroll") for (int j = 0; j < ITEMS; ++j) {            \
-            const double x1 = OPA(j), x2 = OPB(j);                     \
-            RESULT(j, (EXPR))                                          \
-        }                                                              \
-        break;                                                         \
-    }
-#define UN(OPC, EXPR)                                                  \
-    case OPC: {                                                        \
-        _Pragma("unroll") for (int j = 0; j < ITEMS; ++j) {            \
-            const double x1 = OPA(j);                                  \
-            RESULT(j, (EXPR))                                          \
-        }                                                              \
-        break;                                                         \
-    }
-                BIN(OP_ADD, __dadd_rn(x1, x2))
-                BIN(OP_SUB, __dsub_rn(x1, x2))
-                BIN(OP_MUL, __dmul_rn(x1, x2))
-                BIN(OP_DIV, __ddiv_rn(x1, x2))
-                BIN(OP_POW, pow(x1, x2))
-                UN(OP_NEG, -x1)
-                UN(OP_SQRT, __dsqrt_rn(x1))
-                UN(OP_REC, __ddiv_rn(1.0, x1))
-                UN(OP_MOV, x1)
-                UN(OP_SIN, sin(x1))
-                UN(OP_COS, cos(x1))
-                UN(OP_TAN, tan(x1))
-                UN(OP_ASIN, asin(x1))
-                UN(OP_ACOS, acos(x1))
-                UN(OP_ATAN, atan(x1))
-                UN(OP_EXP, exp(x1))
-                UN(OP_LOG, log(x1))
-#undef BIN
-#undef UN
-                case OP_FMA: {
-                    const unsigned cr = (unsigned)(w >> 32) & 0xff;
-                    const int fl = (int)((w >> 40) & 0x3);
-                    const bool cAcc = (w & F_C_ACC) != 0;
+                        for (unsigned u = 0; u < GROUP; ++u) ee[u] = e[q + u * P];
 #pragma unroll
-                    for (int j = 0; j < ITEMS; ++j) {
-                        const double x3 = cAcc ? acc[j] : REG(cr, j);
-                        RESULT(j, dfma(OPA(j), OPB(j), x3, fl))
+                        for (unsigned u = 0; u < GROUP; ++u)
+#pragma unroll
+                            for (int j = 0; j < ITEMS; ++j) v[u][j] = rf.at(field(ee[u], 0), j);
+#pragma unroll
+                        for (unsigned u = 0; u < GROUP; ++u)
+#pragma unroll
+                            for (int j = 0; j < ITEMS; ++j)
+                                if (valid[j]) A.xw[(yoff + (std::uint64_t)(ee[u] >> 8) * n + ii[j]) * S + ss[j]] = v[u][j];
+                    }
+                    for (; q < cnt; q += P) {
+                        const std::uint32_t e0 = e[q];
+#pragma unroll
+                        for (int j = 0; j < ITEMS; ++j)
+                            if (valid[j])
+                                A.xw[(yoff + (std::uint64_t)(e0 >> 8) * n + ii[j]) * S + ss[j]] =
+                                    (flags & H_A_ACC) ? acc[j] : rf.at(field(e0, 0), j);
                     }
                     break;
                 }
                 default: break;
             }
-#undef OPA
-#undef OPB
-#undef RESULT
+            if (P > 1) __syncwarp();
         }
-#undef REG
     }
 }
 
 // Runs the tiles of segments [segBegin, segEnd); a grid barrier separates
 // segments (cooperative launches only when the range holds several segments).
-template <int ITEMS, int LOAD>
+template <int ITEMS, int MODE>
 __global__ void evalKernel(EvalArgs A) {
     extern __shared__ double smem[];
     std::uint64_t* progSmem = reinterpret_cast<std::uint64_t*>(smem);
@@ -294,7 +425,7 @@ __global__ void evalKernel(EvalArgs A) {
                     prog = k.prog;
                 }
             }
-            evalTile<ITEMS, LOAD>(k, prog, regs, t, A);
+            evalTile<ITEMS, MODE>(k, prog, regs, t, A);
         }
         if (sg + 1 < A.segEnd)
             if (!gridBarrier(A.bar, A.hostError, A.timeoutNs)) return;

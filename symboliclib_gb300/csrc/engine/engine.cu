@@ -97,7 +97,7 @@ int uploadPrograms(symgb_unit* u) {
         dk.regs = (std::uint32_t)std::max(1, pr.registers);
         dk.nloads = (std::uint32_t)pr.loads.size();
         dk.nwords = (std::uint32_t)(pr.loads.size() + pr.words.size());
-        dk.pad = 0;
+        dk.litoff = (std::uint32_t)(pr.loads.size() + pr.literalOffset);
         u->hostDevKernels.push_back(dk);
     }
     SYMGB_CUDA(u->devKernels.alloc(u->hostDevKernels.size()));
@@ -113,7 +113,7 @@ int uploadPrograms(symgb_unit* u) {
 // tile boundaries per level (fused schedules) and per kernel (plain schedule).
 int buildTiles(symgb_unit* u) {
     const int S = u->numSets;
-    const int items = u->sched.items_per_tile > 0 ? u->sched.items_per_tile : u->tpb() * u->items();
+    const int items = u->sched.items_per_tile > 0 ? u->sched.items_per_tile : u->launchTpb() / u->lanes() * u->items();
     if (u->tilesSets == S && u->tilesItems == items && u->tilesMath == u->mathIndex()) return SYMGB_OK;
     u->hostTiles.clear();
     u->hostLevelSeg.assign(1, 0);
@@ -149,20 +149,28 @@ std::uint32_t maxRegs(const symgb_unit* u, int level = -1) {
     return r;
 }
 
-// Program words kept in shared memory per CTA (larger programs are read from
-// global memory through the L1 cache).
-constexpr std::uint32_t kProgCapWords = 4096;
-
-std::uint32_t progCap(const symgb_unit* u) { return std::min(u->maxProgWords, kProgCapWords); }
-
-std::size_t smemBytes(const symgb_unit* u, std::uint32_t regs, int items, int tpb) {
-    return (std::size_t)progCap(u) * 8 + (std::size_t)regs * items * tpb * sizeof(double);
+std::uint32_t maxWords(const symgb_unit* u, int level = -1) {
+    std::uint32_t w = 0;
+    for (std::size_t k = 0; k < u->kernels.size(); ++k)
+        if (level < 0 || u->kernels[k].desc.level == level) w = std::max(w, u->hostDevKernels[k].nwords);
+    return w;
 }
 
-// Largest block size <= tpb (a multiple of 32) whose program and register file
-// fit in shared memory; 0 if not even one warp fits.
-int fitBlock(const symgb_unit* u, std::uint32_t regs, int items, int tpb) {
-    while (tpb >= 32 && smemBytes(u, regs, items, tpb) > u->smemOptin) tpb -= 32;
+// Program words that may be staged in shared memory per CTA.  A launch stages
+// its programs whenever they fit beside the register file: read from global
+// memory instead, every bundle header and entry is an L1 access that the
+// gathers compete with, and misses go to L2.  Larger programs are read from
+// global memory (all threads of a warp read the same word).
+constexpr std::uint32_t kProgCapWords = 4096;
+
+std::size_t smemBytes(std::uint32_t progCap, std::uint32_t regs, int items, int tpb, int lanes) {
+    return (std::size_t)progCap * 8 + (std::size_t)regs * items * (tpb / lanes) * sizeof(double);
+}
+
+// Largest block size <= tpb (a multiple of 32) whose register file (and
+// staged program) fit in shared memory; 0 if not even one warp fits.
+int fitBlock(const symgb_unit* u, std::uint32_t progCap, std::uint32_t regs, int items, int tpb, int lanes) {
+    while (tpb >= 32 && smemBytes(progCap, regs, items, tpb, lanes) > u->smemOptin) tpb -= 32;
     return tpb >= 32 ? tpb : 0;
 }
 
@@ -171,19 +179,29 @@ int setSmemLimit(const void* fn, std::size_t bytes) {
     return SYMGB_OK;
 }
 
-const void* evalFunction(int items, bool l2) {
-    switch (items) {
-        case 2: return l2 ? (const void*)evalKernel<2, LOAD_L2> : (const void*)evalKernel<2, LOAD_CACHED>;
-        case 4: return l2 ? (const void*)evalKernel<4, LOAD_L2> : (const void*)evalKernel<4, LOAD_CACHED>;
-        default: return l2 ? (const void*)evalKernel<1, LOAD_L2> : (const void*)evalKernel<1, LOAD_CACHED>;
+const void* evalFunction(int items, bool l2, bool lib) {
+    const int mode = (l2 ? MODE_L2 : 0) | (lib ? MODE_LIB : 0);
+#define SYMGB_EVAL_MODES(I)                                          \
+    switch (mode) {                                                 \
+        case 0: return (const void*)evalKernel<I, 0>;               \
+        case MODE_L2: return (const void*)evalKernel<I, MODE_L2>;   \
+        case MODE_LIB: return (const void*)evalKernel<I, MODE_LIB>; \
+        default: return (const void*)evalKernel<I, MODE_L2 | MODE_LIB>; \
     }
+    switch (items) {
+        case 2: SYMGB_EVAL_MODES(2)
+        case 4: SYMGB_EVAL_MODES(4)
+        default: SYMGB_EVAL_MODES(1)
+    }
+#undef SYMGB_EVAL_MODES
 }
 
 // Enqueues one evaluation on the unit's stream.
 int enqueueRun(symgb_unit* u) {
     if (int e = buildTiles(u)) return e;
     const int items = u->items();
-    const int tpb = u->tpb();
+    const int tpb = u->launchTpb();
+    const int lanes = u->lanes();
     int launches = 0;
     EvalArgs A;
     A.ks = u->devKernels.ptr;
@@ -191,17 +209,26 @@ int enqueueRun(symgb_unit* u) {
     A.x = u->x.ptr;
     A.xw = u->x.ptr;
     A.S = (unsigned)u->numSets;
-    A.progCap = progCap(u);
-    A.regStride = 0;
+    A.lanes = (unsigned)lanes;
     A.bar = u->barrier.ptr;
     A.hostError = u->errorDev;
     A.timeoutNs = u->barrierTimeoutNs;
-    auto launch = [&](bool l2, std::uint32_t regs, unsigned grid, bool coop) -> int {
-        const int bt = fitBlock(u, regs, items, tpb);
+    auto launch = [&](bool l2, std::uint32_t regs, std::uint32_t words, unsigned grid, bool coop) -> int {
+        const void* fn = evalFunction(items, l2, u->usesLibrary);
+        const int bt = fitBlock(u, 0, regs, items, tpb, lanes);
         if (!bt) return fail(SYMGB_ERR_ARGUMENT, "kernel register file exceeds shared memory");
-        const std::size_t smem = smemBytes(u, regs, items, bt);
-        const void* fn = evalFunction(items, l2);
+        const std::array<std::uint32_t, 6> key{(std::uint32_t)l2, regs, words, (std::uint32_t)items, (std::uint32_t)tpb,
+                                                (std::uint32_t)lanes};
+        auto it = u->stagingCache.find(key);
+        if (it == u->stagingCache.end()) {
+            std::uint32_t c = std::min(words, kProgCapWords);
+            if (words > kProgCapWords || fitBlock(u, c, regs, items, tpb, lanes) != bt) c = 0;
+            it = u->stagingCache.emplace(key, c).first;
+        }
+        const std::uint32_t cap = it->second;
+        const std::size_t smem = smemBytes(cap, regs, items, bt, lanes);
         if (setSmemLimit(fn, smem)) return SYMGB_ERR_CUDA;
+        A.progCap = cap;
         if (coop) {
             int perSm = 0;
             SYMGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fn, bt, smem));
@@ -225,7 +252,7 @@ int enqueueRun(symgb_unit* u) {
                 const std::uint32_t k = u->hostTiles[u->hostKernelSeg[sgi]].kernel;
                 A.segBegin = (int)sgi;
                 A.segEnd = (int)sgi + 1;
-                if (int e = launch(false, u->hostDevKernels[k].regs, nt, false)) return e;
+                if (int e = launch(false, u->hostDevKernels[k].regs, u->hostDevKernels[k].nwords, nt, false)) return e;
             }
             break;
         }
@@ -236,15 +263,16 @@ int enqueueRun(symgb_unit* u) {
             const int depth = std::max(1, u->sched.fusion_depth);
             for (int L = 0; L < u->numLevels; L += depth) {
                 const int L1 = std::min(u->numLevels, L + depth);
-                std::uint32_t maxTiles = 0, regs = 1;
+                std::uint32_t maxTiles = 0, regs = 1, words = 0;
                 for (int q = L; q < L1; ++q) {
                     maxTiles = std::max(maxTiles, u->hostLevelSeg[q + 1] - u->hostLevelSeg[q]);
                     regs = std::max(regs, maxRegs(u, q));
+                    words = std::max(words, maxWords(u, q));
                 }
                 if (!maxTiles) continue;
                 A.segBegin = L;
                 A.segEnd = L1;
-                if (int e = launch(L1 - L > 1, regs, maxTiles, L1 - L > 1)) return e;
+                if (int e = launch(L1 - L > 1, regs, words, maxTiles, L1 - L > 1)) return e;
             }
             break;
         }
@@ -255,7 +283,7 @@ int enqueueRun(symgb_unit* u) {
             std::uint32_t maxTiles = 1;
             for (int L = 0; L < u->numLevels; ++L)
                 maxTiles = std::max(maxTiles, u->hostLevelSeg[L + 1] - u->hostLevelSeg[L]);
-            if (int e = launch(true, maxRegs(u), maxTiles, true)) return e;
+            if (int e = launch(true, maxRegs(u), maxWords(u), maxTiles, true)) return e;
             break;
         }
         default: return fail(SYMGB_ERR_ARGUMENT, "unknown schedule kind");
@@ -324,6 +352,7 @@ int copyDesc(symgb_unit* u, const symgb_plan_desc* d) {
         try {
             hk.prog[0] = symgb::engine::compileTemplate(hk.desc, SYMGB_MATH_EXACT);
             hk.prog[1] = symgb::engine::compileTemplate(hk.desc, SYMGB_MATH_FAST);
+            if (hk.prog[0].stats.transcendentals || hk.prog[1].stats.transcendentals) u->usesLibrary = true;
         } catch (const std::exception& ex) {
             return fail(SYMGB_ERR_ARGUMENT, std::string("kernel ") + std::to_string(k) + ": " + ex.what());
         }
@@ -519,6 +548,9 @@ int symgb_set_schedule(symgb_unit_t u, const symgb_schedule* s) {
         return fail(SYMGB_ERR_ARGUMENT, "negative schedule parameter");
     if (s->threads_per_block < 0 || s->threads_per_block > 1024 || (s->threads_per_block % 32))
         return fail(SYMGB_ERR_ARGUMENT, "threads_per_block must be a multiple of 32 up to 1024");
+    if (s->lanes_per_item != 0 && s->lanes_per_item != 1 && s->lanes_per_item != 2 && s->lanes_per_item != 4 &&
+        s->lanes_per_item != 8)
+        return fail(SYMGB_ERR_ARGUMENT, "lanes_per_item must be 1, 2, 4 or 8");
     const bool mathChanged = s->math != u->sched.math;
     u->sched = *s;
     u->dropGraph();
@@ -578,6 +610,8 @@ int symgb_get_stats(symgb_unit_t u, symgb_stats* s) {
         s->gathers += st.gathers * d.num_instances;
         s->max_registers = std::max<std::uint64_t>(s->max_registers, (std::uint64_t)k.prog[mi].registers);
         s->program_words += k.prog[mi].words.size();
+        s->bundles += (std::uint64_t)k.prog[mi].bundles * d.num_instances;
+        s->bundle_entries += (std::uint64_t)k.prog[mi].operations * d.num_instances;
     }
     s->num_intermediates = slots > s->num_outputs ? slots - s->num_outputs : 0;
     return SYMGB_OK;

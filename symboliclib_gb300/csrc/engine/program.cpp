@@ -2,6 +2,7 @@
 #include "program.hpp"
 
 #include <algorithm>
+#include <array>
 #include <cstring>
 #include <functional>
 #include <sstream>
@@ -64,68 +65,11 @@ public:
         }
         scheduleStatements();
         prog_.words.push_back(encode(OP_END, 0, 0, 0, 0));
-        chainThroughAccumulator(prog_.words);
         prog_.registers = maxReg_;
         return std::move(prog_);
     }
 
 private:
-    struct Decoded {
-        std::size_t pos;  // word index
-        int op, d, a, b, c;
-        bool defines;
-        int useA, useB, useC;  // register read through operand a / b / FMA addend, or -1
-    };
-
-    static Decoded decode(const std::vector<std::uint64_t>& w, std::size_t pos) {
-        const std::uint64_t x = w[pos];
-        Decoded I{pos, (int)(x & 0xff), (int)((x >> 8) & 0xff), (int)((x >> 16) & 0xff), (int)((x >> 24) & 0xff),
-                  (int)((x >> 32) & 0xff), false, -1, -1, -1};
-        switch (I.op) {
-            case OP_LDK: I.defines = true; break;
-            case OP_ST: I.useA = I.a; break;
-            case OP_ADD: case OP_SUB: case OP_MUL: case OP_DIV: case OP_POW:
-                I.defines = true; I.useA = I.a; I.useB = I.b; break;
-            case OP_FMA: I.defines = true; I.useA = I.a; I.useB = I.b; I.useC = I.c; break;
-            case OP_END: break;
-            default: I.defines = true; I.useA = I.a; break;  // unary
-        }
-        return I;
-    }
-
-    // A value whose only reader is the next instruction stays in the
-    // accumulator: its producer skips the register-file write and the reader
-    // takes the operand from the accumulator.  Values and their order are
-    // unchanged, only where they are kept.
-    static void chainThroughAccumulator(std::vector<std::uint64_t>& w) {
-        std::vector<Decoded> ins;
-        for (std::size_t pos = 0; pos < w.size();) {
-            ins.push_back(decode(w, pos));
-            pos += ins.back().op == OP_LDK ? 2 : 1;
-        }
-        for (std::size_t i = 0; i + 1 < ins.size(); ++i) {
-            const Decoded& I = ins[i];
-            if (!I.defines) continue;
-            const int r = I.d;
-            int readers = 0;
-            std::size_t first = 0;
-            for (std::size_t j = i + 1; j < ins.size(); ++j) {
-                const Decoded& J = ins[j];
-                if (J.useA == r || J.useB == r || J.useC == r) {
-                    if (!readers) first = j;
-                    ++readers;
-                }
-                if (J.defines && J.d == r) break;
-            }
-            if (readers != 1 || first != i + 1) continue;
-            const Decoded& J = ins[i + 1];
-            w[I.pos] |= F_NOSTORE;
-            if (J.useA == r) w[J.pos] |= F_A_ACC;
-            if (J.useB == r) w[J.pos] |= F_B_ACC;
-            if (J.useC == r) w[J.pos] |= F_C_ACC;
-        }
-    }
-
     const symgb_node& node(int j) const { return k_.nodes[j]; }
 
     // Key of a load leaf: kind (1 gather, 2 constant) in bits 62-63.
@@ -420,7 +364,7 @@ private:
             const symgb_node& out = node(kids_[j][0]);
             if (out.op != N_VAR || out.b != G_OUTPUT) throw std::runtime_error("ASSIGN to a non-output");
             if (out.a < 0 || (std::uint32_t)out.a >= k_.num_output_rows) throw std::runtime_error("output row out of range");
-            if ((std::uint32_t)out.a >= ST_ROW_LIMIT) throw std::runtime_error("more than 2^24 output rows");
+            if ((std::uint32_t)out.a >= ENTRY_FIELD_LIMIT) throw std::runtime_error("more than 2^24 output rows");
             Val v = expr(kids_[j][1]);
             emit(encode(OP_ST, 0, v.reg, 0, (std::uint32_t)out.a));
             ++prog_.stats.stores;
@@ -442,41 +386,296 @@ private:
     Program prog_;
 };
 
+
+// ------------------------------------------------------------------ bundling
+
+struct LinOp {
+    int op = OP_END;
+    int d = -1;             // register written in the linear code, -1 if none
+    int src[3] = {-1, -1, -1};
+    int nsrc = 0;
+    std::uint32_t row = 0;  // OP_ST
+    std::uint64_t lit = 0;  // OP_LDK
+};
+
+bool isBinary(int op) { return op == OP_ADD || op == OP_SUB || op == OP_MUL || op == OP_DIV || op == OP_POW; }
+bool isFma(int op) { return op == OP_FMA || op == OP_FMS || op == OP_FNMA || op == OP_FNMS; }
+
+std::vector<LinOp> parseLinear(const std::vector<std::uint64_t>& w) {
+    std::vector<LinOp> ops;
+    for (std::size_t pc = 0; pc < w.size();) {
+        const std::uint64_t x = w[pc++];
+        const int op = (int)(x & 0xff);
+        if (op == OP_END) break;
+        const int d = (int)((x >> 8) & 0xff), a = (int)((x >> 16) & 0xff), b = (int)((x >> 24) & 0xff);
+        LinOp L;
+        L.op = op;
+        switch (op) {
+            case OP_LDK:
+                L.d = d;
+                if (pc >= w.size()) throw std::runtime_error("truncated literal");
+                L.lit = w[pc++];
+                break;
+            case OP_ST:
+                L.src[0] = a;
+                L.nsrc = 1;
+                L.row = (std::uint32_t)((x >> 32) & 0xffffff);
+                break;
+            case OP_FMA: {
+                static const int byFlags[4] = {OP_FMA, OP_FNMA, OP_FMS, OP_FNMS};
+                L.op = byFlags[(x >> 40) & 3];
+                L.d = d;
+                L.src[0] = a;
+                L.src[1] = b;
+                L.src[2] = (int)((x >> 32) & 0xff);
+                L.nsrc = 3;
+                break;
+            }
+            default:
+                L.d = d;
+                L.src[0] = a;
+                L.nsrc = 1;
+                if (isBinary(op)) {
+                    L.src[1] = b;
+                    L.nsrc = 2;
+                }
+        }
+        ops.push_back(L);
+    }
+    return ops;
+}
+
+// Schedules the linear code into bundles and assigns registers (see the
+// description of the program format).
+Program bundle(const Program& lin, int window) {
+    const std::vector<LinOp> ops = parseLinear(lin.words);
+    const int n = (int)ops.size();
+    const int nl = (int)lin.loads.size();
+
+    // Value numbering: loads are values 0..nl-1, then one value per definition.
+    std::vector<int> cur(256, -1);
+    for (int i = 0; i < nl; ++i) cur[(lin.loads[i] >> 8) & 0xff] = i;
+    std::vector<int> defOf(n, -1), producer(nl, -1);
+    std::vector<std::array<int, 3>> use(n, {-1, -1, -1});
+    std::vector<std::vector<int>> deps(n);
+    std::unordered_map<std::uint32_t, int> lastStore;
+    for (int j = 0; j < n; ++j) {
+        const LinOp& L = ops[j];
+        for (int s = 0; s < L.nsrc; ++s) {
+            const int v = cur[L.src[s]];
+            if (v < 0) throw std::runtime_error("program reads a register before writing it");
+            use[j][s] = v;
+            if (producer[v] >= 0) deps[j].push_back(producer[v]);
+        }
+        if (L.op == OP_ST) {  // two stores to one output keep their order
+            auto it = lastStore.find(L.row);
+            if (it != lastStore.end()) deps[j].push_back(it->second);
+            lastStore[L.row] = j;
+        }
+        if (L.d >= 0) {
+            defOf[j] = (int)producer.size();
+            producer.push_back(j);
+            cur[L.d] = defOf[j];
+        }
+    }
+    const int nv = (int)producer.size();
+
+    // List scheduling: among the next `window` unscheduled operations, take
+    // every ready operation of the most frequent opcode as one bundle.
+    std::vector<int> bundleOf(n, -1);
+    std::vector<std::vector<int>> bundles;
+    int frontier = 0;
+    std::vector<std::vector<int>> byOp(NUM_OPCODES);
+    while (frontier < n) {
+        for (auto& v : byOp) v.clear();
+        int firstOp = -1;
+        for (int j = frontier, seen = 0; j < n && seen < std::max(1, window); ++j) {
+            if (bundleOf[j] >= 0) continue;
+            ++seen;
+            bool ready = true;
+            for (int p : deps[j])
+                if (bundleOf[p] < 0) {
+                    ready = false;
+                    break;
+                }
+            if (!ready) continue;
+            byOp[ops[j].op].push_back(j);
+            if (firstOp < 0) firstOp = ops[j].op;
+        }
+        int best = firstOp;
+        for (int o = 0; o < NUM_OPCODES; ++o)
+            if (byOp[o].size() > byOp[best].size()) best = o;
+        std::vector<int>& chosen = byOp[best];
+        if (chosen.size() > 0xffff) chosen.resize(0xffff);
+        const int b = (int)bundles.size();
+        for (int j : chosen) bundleOf[j] = b;
+        bundles.push_back(chosen);
+        while (frontier < n && bundleOf[frontier] >= 0) ++frontier;
+    }
+
+    // Accumulator forwarding between consecutive single-entry bundles: a value
+    // whose every read is in the next bundle stays in the accumulator.
+    const int nb = (int)bundles.size();
+    auto viaBundle = [](int op) {  // operations the interpreter runs through runBundle
+        return op == OP_LDK || op == OP_ADD || op == OP_SUB || op == OP_MUL || op == OP_DIV || op == OP_NEG ||
+               op == OP_MOV || op == OP_SQRT || op == OP_REC || isFma(op);
+    };
+    std::vector<int> useCount(nv, 0);
+    for (int j = 0; j < n; ++j)
+        for (int s = 0; s < ops[j].nsrc; ++s) ++useCount[use[j][s]];
+    std::vector<std::uint32_t> headerFlags(nb, 0);
+    std::vector<char> inAccOnly(nv, 0);
+    for (int b = 0; b + 1 < nb; ++b) {
+        if (bundles[b].size() != 1 || bundles[b + 1].size() != 1) continue;
+        const int j = bundles[b][0], k = bundles[b + 1][0];
+        const int v = defOf[j];
+        if (v < 0 || !viaBundle(ops[j].op) || !(viaBundle(ops[k].op) || ops[k].op == OP_ST) || ops[k].op == OP_LDK)
+            continue;
+        int here = 0;
+        std::uint32_t f = 0;
+        for (int s = 0; s < ops[k].nsrc; ++s)
+            if (use[k][s] == v) {
+                ++here;
+                f |= H_A_ACC << s;
+            }
+        if (here == 0 || here != useCount[v]) continue;
+        headerFlags[b + 1] |= f;
+        headerFlags[b] |= H_NOSTORE;
+        inAccOnly[v] = 1;
+    }
+
+    // Registers: a value occupies its register from its defining bundle (or the
+    // load section) through its last reading bundle.
+    std::vector<int> lastUse(nv, -1);
+    for (int j = 0; j < n; ++j)
+        for (int s = 0; s < ops[j].nsrc; ++s) lastUse[use[j][s]] = std::max(lastUse[use[j][s]], bundleOf[j]);
+    std::vector<std::vector<int>> freeAfter(nb + 1);
+    std::vector<int> slot(nv, -1), pool;
+    int nregs = 0;
+    auto alloc = [&]() {
+        if (!pool.empty()) {
+            const int r = pool.back();
+            pool.pop_back();
+            return r;
+        }
+        if (nregs >= MAX_REGISTERS) throw std::runtime_error("template needs more than 255 live values");
+        return nregs++;
+    };
+    for (int v = 0; v < nl; ++v) {
+        slot[v] = alloc();
+        freeAfter[std::max(0, lastUse[v])].push_back(v);
+    }
+    Program out;
+    out.stats = lin.stats;
+    for (int b = 0; b < nb; ++b) {
+        for (int j : bundles[b])
+            if (defOf[j] >= 0) {
+                const int v = defOf[j];
+                if (inAccOnly[v]) {
+                    slot[v] = 0;  // never written to the register file
+                    continue;
+                }
+                slot[v] = alloc();
+                freeAfter[std::max(b, lastUse[v])].push_back(v);
+            }
+        for (int v : freeAfter[b]) pool.push_back(slot[v]);
+    }
+    out.registers = nregs;
+
+    for (int i = 0; i < nl; ++i)
+        out.loads.push_back((lin.loads[i] & ~0xff00ull) | ((std::uint64_t)slot[i] << 8));
+
+    std::vector<std::uint64_t> literals;
+    std::unordered_map<std::uint64_t, std::uint32_t> literalIndex;
+    for (int b = 0; b < nb; ++b) {
+        const auto& B = bundles[b];
+        const int op = ops[B[0]].op;
+        out.words.push_back((std::uint64_t)op | ((std::uint64_t)B.size() << 8) | headerFlags[b]);
+        std::uint64_t pair = 0;
+        for (std::size_t q = 0; q < B.size(); ++q) {
+            const int j = B[q];
+            const LinOp& L = ops[j];
+            std::uint32_t e = 0;
+            if (op == OP_ST) {
+                e = (std::uint32_t)slot[use[j][0]] | (L.row << 8);
+            } else if (op == OP_LDK) {
+                auto it = literalIndex.find(L.lit);
+                if (it == literalIndex.end()) {
+                    it = literalIndex.emplace(L.lit, (std::uint32_t)literals.size()).first;
+                    literals.push_back(L.lit);
+                }
+                if (it->second >= ENTRY_FIELD_LIMIT) throw std::runtime_error("too many literals");
+                e = (std::uint32_t)slot[defOf[j]] | (it->second << 8);
+            } else {
+                e = (std::uint32_t)slot[defOf[j]];
+                for (int s = 0; s < L.nsrc; ++s) e |= (std::uint32_t)slot[use[j][s]] << (8 * (s + 1));
+            }
+            if (q & 1) {
+                out.words.push_back(pair | ((std::uint64_t)e << 32));
+            } else {
+                pair = e;
+                if (q + 1 == B.size()) out.words.push_back(pair);
+            }
+        }
+        out.operations += (int)B.size();
+    }
+    out.bundles = nb;
+    out.words.push_back(OP_END);
+    out.literalOffset = (std::uint32_t)out.words.size();
+    out.words.insert(out.words.end(), literals.begin(), literals.end());
+    return out;
+}
+
 }  // namespace
 
-Program compileTemplate(const symgb_kernel_desc& k, int math) {
+Program compileTemplate(const symgb_kernel_desc& k, int math, int window) {
     Compiler c(k, math);
-    return c.run();
+    Program linear = c.run();
+    return bundle(linear, window);
 }
 
 std::string disassemble(const Program& p) {
-    static const char* names[NUM_OPCODES] = {"end", "ldx", "ldc", "ldk", "st", "add", "sub", "mul", "div", "neg", "sqrt",
-                                             "rec", "fma", "sin", "cos", "tan", "asin", "acos", "atan", "exp", "log",
-                                             "pow", "mov"};
+    static const char* names[NUM_OPCODES] = {"end", "ldx", "ldc", "ldk", "st", "add", "sub", "mul", "div",
+                                             "neg", "sqrt", "rec", "fma", "sin", "cos", "tan", "asin", "acos",
+                                             "atan", "exp", "log", "pow", "mov", "fms", "fnma", "fnms"};
     std::ostringstream os;
-    std::vector<std::uint64_t> all(p.loads);
-    all.insert(all.end(), p.words.begin(), p.words.end());
-    for (std::size_t pc = 0; pc < all.size(); ++pc) {
-        const std::uint64_t w = all[pc];
-        const int op = (int)(w & 0xff), d = (int)((w >> 8) & 0xff), a = (int)((w >> 16) & 0xff),
-                  b = (int)((w >> 24) & 0xff);
+    for (std::uint64_t w : p.loads) {
+        const int op = (int)(w & 0xff), d = (int)((w >> 8) & 0xff);
         const std::int32_t imm = (std::int32_t)(w >> 32);
-        os << (op < NUM_OPCODES ? names[op] : "?") << " ";
-        switch (op) {
-            case OP_LDX: os << "r" << d << " row" << ((w >> 16) & 0xffff) << " off" << imm; break;
-            case OP_LDC: os << "r" << d << " crow" << imm; break;
-            case OP_LDK: {
+        if (op == OP_LDX)
+            os << "ldx r" << d << " row" << ((w >> 16) & 0xffff) << " off" << imm << "\n";
+        else
+            os << "ldc r" << d << " crow" << imm << "\n";
+    }
+    for (std::size_t pc = 0; pc < p.words.size();) {
+        const std::uint64_t h = p.words[pc++];
+        const int op = (int)(h & 0xff);
+        if (op == OP_END) break;
+        const unsigned cnt = (unsigned)((h >> 8) & 0xffff);
+        os << (op < NUM_OPCODES ? names[op] : "?") << " x" << cnt;
+        if (h & H_A_ACC) os << " a=acc";
+        if (h & H_B_ACC) os << " b=acc";
+        if (h & H_C_ACC) os << " c=acc";
+        if (h & H_NOSTORE) os << " nostore";
+        os << ":";
+        for (unsigned q = 0; q < cnt; ++q) {
+            const std::uint32_t e = (std::uint32_t)(p.words[pc + q / 2] >> (32 * (q & 1)));
+            const unsigned f0 = e & 0xff, f1 = (e >> 8) & 0xff, f2 = (e >> 16) & 0xff, f3 = e >> 24;
+            os << " [";
+            if (op == OP_ST) {
+                os << "y" << (e >> 8) << "=r" << f0;
+            } else if (op == OP_LDK) {
                 double v;
-                std::memcpy(&v, &all[pc + 1], 8);
-                os << "r" << d << " " << v;
-                ++pc;
-                break;
+                std::memcpy(&v, &p.words[p.literalOffset + (e >> 8)], 8);
+                os << "r" << f0 << "=" << v;
+            } else {
+                os << "r" << f0 << "=r" << f1;
+                if (isBinary(op) || isFma(op)) os << ",r" << f2;
+                if (isFma(op)) os << ",r" << f3;
             }
-            case OP_ST: os << "y" << ((w >> 32) & 0xffffff) << " r" << a; break;
-            case OP_FMA: os << "r" << d << " r" << a << " r" << b << " r" << (imm & 0xff) << " f" << (imm >> 8); break;
-            default: os << "r" << d << " r" << a << " r" << b;
+            os << "]";
         }
-        if (w >> 56) os << " acc" << (w >> 56);
+        pc += (cnt + 1) / 2;
         os << "\n";
     }
     return os.str();

@@ -2,14 +2,20 @@
 // a ComputeKernel template.
 //
 // A template (post-order nodes of a BLOCK of DEFINE / ASSIGN statements) is
-// compiled into a linear sequence of 64-bit instructions over a per-thread
-// register file.  Every thread runs the same program for its own instance and
-// value set, so instruction fetch and decode are warp-uniform.  In exact mode
-// each template operation is one rounded operation in the template's order
-// (n-ary sums and products left to right, as C evaluates the reference's
-// generated code), so results are bit-identical to the reference compiled
-// without FP contraction.  In fast mode, products feeding a sum are fused into
-// FMA.
+// first compiled into a linear sequence of operations over virtual registers.
+// In exact mode each template operation is one rounded operation in the
+// template's order (n-ary sums and products left to right, as C evaluates the
+// reference's generated code), so results are bit-identical to the reference
+// compiled without FP contraction.  In fast mode, products feeding a sum are
+// fused into FMA.
+//
+// The linear code is then list-scheduled into bundles: a bundle applies one
+// operation to many independent operand tuples (no entry reads another
+// entry's result), so the interpreter decodes one header per bundle and keeps
+// several FP64 operations of one thread in flight.  Registers are assigned
+// after scheduling; a register freed by a bundle is reused only by later
+// bundles.  Scheduling only reorders operations whose inputs are ready, so
+// every value is computed by the same operations on the same operands.
 #pragma once
 #include <cstdint>
 #include <string>
@@ -20,13 +26,19 @@
 namespace symgb {
 namespace engine {
 
-// Instruction word: op (bits 0-7), dst (8-15), a (16-23), b (24-31), imm (32-63).
+// Load-section word: op (bits 0-7), dst (8-15), imm (32-63), see OP_LDX/OP_LDC.
+// Compute bundle: header word (op bits 0-7, entry count bits 8-23, accumulator
+// flags bits 24-27), then the
+// 32-bit entries, two per word (entry 2q in the low half of word q).  Entry
+// fields: d bits 0-7, a 8-15, b 16-23, c 24-31; OP_ST entries hold the source
+// register in bits 0-7 and the output row in bits 8-31; OP_LDK entries hold d
+// and the index of the literal in the program's literal table in bits 8-31.
 enum Opcode : std::uint8_t {
     OP_END = 0,
     OP_LDX = 1,   // r[dst] = x[p[row * n + i] + off]; row = bits 16-31, off = imm (signed)
     OP_LDC = 2,   // r[dst] = c[row * n + i]; row = imm
-    OP_LDK = 3,   // r[dst] = next word as double
-    OP_ST = 4,    // y[row * n + i] = r[a]; row = imm
+    OP_LDK = 3,   // r[d] = literal
+    OP_ST = 4,    // y[row * n + i] = r[a]
     OP_ADD = 5,
     OP_SUB = 6,   // r[a] - r[b]  (== r[a] + -(r[b]) exactly)
     OP_MUL = 7,
@@ -34,7 +46,7 @@ enum Opcode : std::uint8_t {
     OP_NEG = 9,
     OP_SQRT = 10,
     OP_REC = 11,  // 1 / r[a]
-    OP_FMA = 12,  // r[dst] = (+-)(r[a] * r[b]) (+-) r[c]; c = bits 32-39, flags bits 40-41
+    OP_FMA = 12,  // r[d] = r[a] * r[b] + r[c], one rounding
     OP_SIN = 13,
     OP_COS = 14,
     OP_TAN = 15,
@@ -45,6 +57,9 @@ enum Opcode : std::uint8_t {
     OP_LOG = 20,
     OP_POW = 21,
     OP_MOV = 22,
+    OP_FMS = 23,   // r[a] * r[b] - r[c]
+    OP_FNMA = 24,  // -(r[a] * r[b]) + r[c]
+    OP_FNMS = 25,  // -(r[a] * r[b]) - r[c]
     NUM_OPCODES
 };
 
@@ -52,15 +67,17 @@ constexpr int FMA_NEG_PRODUCT = 1;
 constexpr int FMA_NEG_ADDEND = 2;
 constexpr int MAX_REGISTERS = 255;
 
-// Accumulator flags, bits 56-63 of a compute word.  The interpreter keeps the
-// result of every instruction in a hardware register (the accumulator); a
-// value consumed only by the very next instruction is passed there instead of
-// through the shared-memory register file.
-constexpr std::uint64_t F_A_ACC = 1ull << 56;    // operand a is the accumulator
-constexpr std::uint64_t F_B_ACC = 2ull << 56;    // operand b is the accumulator
-constexpr std::uint64_t F_C_ACC = 4ull << 56;    // FMA addend is the accumulator
-constexpr std::uint64_t F_NOSTORE = 8ull << 56;  // result only in the accumulator
-constexpr std::uint32_t ST_ROW_LIMIT = 1u << 24; // OP_ST row field: bits 32-55
+constexpr std::uint32_t ENTRY_FIELD_LIMIT = 1u << 24;  // OP_ST row / OP_LDK literal index
+
+// Accumulator flags, header bits 24-27, set only on single-entry bundles.  The
+// interpreter keeps the result of every single-entry bundle in a hardware
+// register (the accumulator); a value whose only reader is the next bundle,
+// itself a single entry, is passed there instead of through the shared-memory
+// register file.  Values and their order are unchanged, only where they live.
+constexpr std::uint32_t H_A_ACC = 1u << 24;     // operand a (ST: the stored value) is the accumulator
+constexpr std::uint32_t H_B_ACC = 1u << 25;     // operand b is the accumulator
+constexpr std::uint32_t H_C_ACC = 1u << 26;     // FMA addend is the accumulator
+constexpr std::uint32_t H_NOSTORE = 1u << 27;   // the result stays in the accumulator only
 
 struct ProgramStats {
     std::uint64_t flops = 0, divs = 0, sqrts = 0, transcendentals = 0, gathers = 0, constLoads = 0, stores = 0;
@@ -69,20 +86,29 @@ struct ProgramStats {
 // A program has two sections.  `loads` holds every distinct gather (LDX) and
 // per-instance constant read (LDC) of the template, each loaded once into its
 // own register before any arithmetic, so the interpreter can issue them all
-// back to back.  `words` holds the arithmetic, literal loads (LDK) and output
-// stores, ending with OP_END.
+// back to back.  `words` holds the compute bundles (arithmetic, literal loads
+// and output stores), an OP_END word, then the literal table (one double per
+// word) starting at word `literalOffset`.
 struct Program {
     std::vector<std::uint64_t> loads;
     std::vector<std::uint64_t> words;
+    std::uint32_t literalOffset = 0;
     int registers = 0;
+    int bundles = 0;      // compute bundles
+    int operations = 0;   // compute entries over all bundles
     ProgramStats stats;
 };
+
+// Operations a bundle may gather from: the next `window` not yet scheduled
+// operations of the linear code (larger windows give larger bundles and more
+// live registers).
+constexpr int BUNDLE_WINDOW = 64;
 
 // Compiles one kernel template.  Throws std::runtime_error on templates the
 // engine cannot execute (unknown operations, more than MAX_REGISTERS live
 // values).  Loads are deduplicated: a gather that the template reads several
 // times is loaded once; the value is the same, so results do not change.
-Program compileTemplate(const symgb_kernel_desc& k, int math);
+Program compileTemplate(const symgb_kernel_desc& k, int math, int window = BUNDLE_WINDOW);
 
 // Human-readable listing (tests and debugging).
 std::string disassemble(const Program& p);

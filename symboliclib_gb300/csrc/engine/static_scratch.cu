@@ -170,7 +170,7 @@ extern "C" int symgb_run_static(symgb_unit_t u, const uint32_t* index_data, cons
         dk.regs = (std::uint32_t)std::max(1, pr.registers);
         dk.nloads = (std::uint32_t)pr.loads.size();
         dk.nwords = (std::uint32_t)(pr.loads.size() + pr.words.size());
-        dk.pad = 0;
+        dk.litoff = (std::uint32_t)(pr.loads.size() + pr.literalOffset);
         dks.push_back(dk);
     }
 
@@ -196,8 +196,14 @@ extern "C" int symgb_run_static(symgb_unit_t u, const uint32_t* index_data, cons
         while (bt >= 32 && smemFor(bt) > (std::size_t)optin) bt -= 32;
         if (bt < 32) return failStatic(SYMGB_ERR_ARGUMENT, "kernel register file exceeds shared memory");
         const std::size_t smem = smemFor(bt);
-        const void* fn = items == 4 ? (const void*)evalKernel<4, LOAD_L2>
-                                    : items == 2 ? (const void*)evalKernel<2, LOAD_L2> : (const void*)evalKernel<1, LOAD_L2>;
+        const void* fn;
+        if (u->usesLibrary)
+            fn = items == 4 ? (const void*)evalKernel<4, MODE_L2 | MODE_LIB>
+                            : items == 2 ? (const void*)evalKernel<2, MODE_L2 | MODE_LIB>
+                                         : (const void*)evalKernel<1, MODE_L2 | MODE_LIB>;
+        else
+            fn = items == 4 ? (const void*)evalKernel<4, MODE_L2>
+                            : items == 2 ? (const void*)evalKernel<2, MODE_L2> : (const void*)evalKernel<1, MODE_L2>;
         if (smem > 48 * 1024) STATIC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int perSm = 0;
         STATIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fn, bt, smem));
@@ -215,7 +221,7 @@ extern "C" int symgb_run_static(symgb_unit_t u, const uint32_t* index_data, cons
         A.xw = x;
         A.S = 1;
         A.progCap = progCap;
-        A.regStride = 0;
+        A.lanes = 1;
         A.bar = reinterpret_cast<BarrierState*>(base + oBar);
         A.hostError = reinterpret_cast<int*>(base + oBar + sizeof(BarrierState));
         A.timeoutNs = u->barrierTimeoutNs;

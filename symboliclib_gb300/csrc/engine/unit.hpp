@@ -3,7 +3,10 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <array>
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -57,8 +60,9 @@ struct symgb_unit {
     std::uint64_t numTotalMemory = 0, numIndices = 0, numOutputValues = 0, numConstants = 0;
     int threadsPerBlock = 128;
     int numLevels = 0;
-    symgb_schedule sched{SYMGB_SCHEDULE_PLAIN, SYMGB_MATH_FAST, 0, 0, 0, 0, 1};
+    symgb_schedule sched{SYMGB_SCHEDULE_PLAIN, SYMGB_MATH_FAST, 0, 0, 0, 0, 1, 0, 1};
     int numSets = 1;
+    bool usesLibrary = false;  // some program calls pow, sin, ... (interpreter variant MODE_LIB)
 
     // device state
     bool initialized = false;
@@ -79,6 +83,9 @@ struct symgb_unit {
     std::vector<std::uint32_t> hostLevelSeg, hostKernelSeg;  // tile boundaries per level / per kernel
     std::vector<Tile> hostTiles;
     std::uint32_t maxProgWords = 0;
+    // program words staged in shared memory, per (L2 loads, registers, program
+    // words, items per thread, threads per block, lanes per item) of a launch
+    std::map<std::array<std::uint32_t, 6>, std::uint32_t> stagingCache;
     std::size_t tilesFor = 0;  // configuration the tile table was built for
     int tilesSets = -1, tilesItems = -1, tilesMath = -1;
     cudaGraphExec_t graph = nullptr;
@@ -121,5 +128,8 @@ struct symgb_unit {
     int mathIndex() const { return sched.math == SYMGB_MATH_EXACT ? 0 : 1; }
     int tpb() const { return sched.threads_per_block > 0 ? sched.threads_per_block : threadsPerBlock; }
     int items() const { return sched.items_per_thread == 2 || sched.items_per_thread == 4 ? sched.items_per_thread : 1; }
+    int lanes() const { return sched.lanes_per_item > 1 ? sched.lanes_per_item : 1; }
+    // Block size of a launch: whole warps when several lanes share an item.
+    int launchTpb() const { return lanes() > 1 ? std::max(32, tpb() / 32 * 32) : tpb(); }
 };
 

@@ -37,14 +37,14 @@ class PlanDesc(C.Structure):
 class Schedule(C.Structure):
     _fields_ = [("kind", C.c_int32), ("math", C.c_int32), ("threads_per_block", C.c_int32),
                 ("items_per_tile", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32),
-                ("items_per_thread", C.c_int32), ("fusion_depth", C.c_int32)]
+                ("items_per_thread", C.c_int32), ("fusion_depth", C.c_int32), ("lanes_per_item", C.c_int32)]
 
 
 class Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("num_kernels", "num_levels", "num_inputs", "num_outputs",
                                            "num_intermediates", "index_entries", "constant_entries", "flops",
                                            "divs", "sqrts", "transcendentals", "gathers", "max_registers",
-                                           "program_words")]
+                                           "program_words", "bundles", "bundle_entries")]
 
 
 # Every function declared in include/symgb.h, with its ctypes signature.
@@ -225,9 +225,9 @@ class Unit:
         return cls(w.plan, w.index_data, w.out_index_data, w.const_data)
 
     def set_schedule(self, kind=SCHEDULE_PLAIN, math=MATH_FAST, threads_per_block=0, items_per_tile=0,
-                     blocks_per_sm=0, use_graph=0, items_per_thread=1, fusion_depth=0) -> None:
+                     blocks_per_sm=0, use_graph=0, items_per_thread=1, fusion_depth=0, lanes_per_item=1) -> None:
         s = Schedule(kind, math, threads_per_block, items_per_tile, blocks_per_sm, use_graph, items_per_thread,
-                     fusion_depth)
+                     fusion_depth, lanes_per_item)
         check(self._lib.symgb_set_schedule(self.handle, C.byref(s)))
 
     def set_num_sets(self, n: int) -> None:

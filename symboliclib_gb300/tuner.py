@@ -28,15 +28,20 @@ class Sched:
     kind: str
     items: int
     tpb: int
-    tile: int  # tile = tpb * items * tile work items
+    tile: int  # a tile is (tpb / lanes) * items * tile work items
+    lanes: int = 1
 
     def apply(self, unit: native.Unit, math_mode: int = native.MATH_FAST, graph: int = 1) -> None:
         k, depth = KINDS[self.kind]
-        unit.set_schedule(kind=k, math=math_mode, threads_per_block=self.tpb, items_per_tile=self.tpb * self.items * self.tile,
-                          items_per_thread=self.items, use_graph=graph, fusion_depth=depth)
+        unit.set_schedule(kind=k, math=math_mode, threads_per_block=self.tpb,
+                          items_per_tile=self.tpb // self.lanes * self.items * self.tile, items_per_thread=self.items,
+                          use_graph=graph, fusion_depth=depth, lanes_per_item=self.lanes)
 
 
-SPACE = [Sched(k, i, t, f) for k, i, t, f in itertools.product(KINDS, (1, 2, 4), (64, 128, 256), (1, 4))]
+# (items per thread, lanes per item): several items per thread for small
+# register files, several lanes per item for large ones
+SHAPES = ((1, 1), (2, 1), (4, 1), (1, 2), (1, 4))
+SPACE = [Sched(k, i, t, f, l) for k, (i, l), t, f in itertools.product(KINDS, SHAPES, (64, 128, 256), (1, 4))]
 DEFAULT = Sched("levels", 1, 128, 1)
 
 
@@ -101,19 +106,22 @@ def plan_features(stats: native.Stats, num_sets: int) -> np.ndarray:
         lg(stats.flops * S), lg((stats.divs + stats.sqrts) * S), lg(stats.gathers * S),
         lg(stats.index_entries), lg(stats.constant_entries), float(stats.num_kernels), float(stats.num_levels),
         float(stats.max_registers), lg(stats.program_words), lg(S),
+        lg(stats.bundles * S), float(stats.bundle_entries) / max(1.0, float(stats.bundles)),
     ], np.float32)
 
 
 def schedule_features(s: Sched) -> np.ndarray:
     onehot = [1.0 if s.kind == k else 0.0 for k in KINDS]
-    return np.array(onehot + [math.log2(s.items), math.log2(s.tpb), math.log2(s.tile)], np.float32)
+    return np.array(onehot + [math.log2(s.lanes), math.log2(s.items), math.log2(s.tpb), math.log2(s.tile)], np.float32)
 
 
 def features(stats: native.Stats, num_sets: int, s: Sched) -> np.ndarray:
     p = plan_features(stats, num_sets)
     q = schedule_features(s)
     # interactions: work per launch under this schedule
-    return np.concatenate([p, q, p[:6] * q[-3] / 8.0, p[:6] * q[-2] / 8.0])
+    # register file bytes per thread under this shape (occupancy)
+    regfile = np.array([math.log2(1.0 + float(stats.max_registers) * s.items / s.lanes)], np.float32)
+    return np.concatenate([p, q, p[:6] * q[-3] / 8.0, p[:6] * q[-2] / 8.0, p[:6] * q[-4] / 8.0, regfile])
 
 
 class CostModel:

@@ -77,6 +77,8 @@ def test_schedule_validation():
     assert lib.symgb_set_schedule(h, C.byref(bad)) == -1
     bad = native.Schedule(0, 0, 100, 0, 0, 0)  # not a multiple of 32
     assert lib.symgb_set_schedule(h, C.byref(bad)) == -1
+    bad = native.Schedule(0, 0, 64, 0, 0, 0, 1, 0, 3)  # lanes per item not a power of two up to 8
+    assert lib.symgb_set_schedule(h, C.byref(bad)) == -1
     ok = native.Schedule(2, 0, 64, 0, 0, 0)
     native.check(lib.symgb_set_schedule(h, C.byref(ok)))
     got = native.Schedule()

@@ -117,6 +117,32 @@ def test_block_sizes_and_items_per_thread(tpb, items):
                 assert bits_equal(u.get_result(0), gold), (name, kind, tile)
 
 
+@pytest.mark.parametrize("lanes", [2, 4, 8])
+@pytest.mark.parametrize("tpb", [32, 128])
+def test_lanes_per_item(lanes, tpb):
+    """Several threads per work item split its bundles: results unchanged, for
+    every schedule, partial tiles and several value sets."""
+    for name, size, seed in [("cotan", 8, 22), ("cloth", 5, 32), ("neohookean", 2, 42)]:
+        _, inp, gold = load_golden(name, size)
+        w = native.Workload(name, size, seed)
+        u = native.Unit.from_workload(w)
+        for kind in SCHEDULES:
+            for tile in (0, 3 * tpb // lanes + 1):
+                u.set_schedule(kind=kind, math=native.MATH_EXACT, threads_per_block=tpb, items_per_tile=tile,
+                               lanes_per_item=lanes)
+                u.set_num_sets(1)
+                for i, a in enumerate(split_inputs(w, inp)):
+                    u.set_arg(i, a)
+                u.run()
+                assert bits_equal(u.get_result(0), gold), (name, kind, tile)
+        u.set_num_sets(5)
+        for i, a in enumerate(split_inputs(w, inp)):
+            u.set_arg(i, np.tile(a, 5))
+        u.run()
+        out = u.get_result(0).reshape(5, -1)
+        assert bits_equal(out[0], gold) and bits_equal(out[4], gold), name
+
+
 def test_larger_cases_match_oracle():
     """Sizes beyond the fixtures: engine exact mode vs the CPU oracle."""
     for name, size, seed in [("cotan", 60, 5), ("ata", 30, 6), ("cloth", 12, 7)]:
