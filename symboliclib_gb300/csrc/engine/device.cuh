@@ -53,7 +53,7 @@ struct EvalArgs {
     double* xw;
     unsigned S;
     unsigned progCap;               // program words that fit in shared memory (0: read from global)
-    unsigned lanes;                 // threads per work item (1, 2, 4 or 8)
+    unsigned reserved;
     BarrierState* bar;
     int* hostError;
     unsigned long long timeoutNs;
@@ -139,48 +139,55 @@ struct RegFile {
     __device__ __forceinline__ double& at(unsigned r, int j) const { return R[r * stride + j * T]; }
 };
 
-// Runs the entries lane, lane + P, lane + 2P, ... of a bundle (P = lanes per
-// work item; the other lanes of the item run the rest).
-// Single-entry bundles may take operands from, and leave their result only in,
-// the accumulator `acc` (header flags; see program.hpp).
-template <int ITEMS, int NSRC, unsigned GROUP, class F>
-__device__ __forceinline__ void runBundle(const std::uint32_t* e, unsigned cnt, const RegFile& rf, unsigned lane,
-                                          unsigned P, unsigned flags, double (&acc)[ITEMS], F f) {
-    unsigned q = lane;
-    for (; q + (GROUP - 1) * P < cnt; q += GROUP * P) {
-        std::uint32_t ee[GROUP];
+// Runs a bundle of `cnt` entries on the P lanes of each work item.  Round r
+// gives lane l entry r * P + l; rounds are processed four, then two, then one
+// at a time, the same count on every lane of the warp.  A lane whose entry
+// index passes the end takes the last entry instead: it computes the same
+// value into the same register as that entry's own lane, which is harmless,
+// and keeps every lane on one instruction stream.  Single-entry bundles may
+// take operands from, and leave their result only in, the accumulator `acc`
+// (header flags; see program.hpp).
+template <int ITEMS, int NSRC, unsigned G, class F>
+__device__ __forceinline__ void runGroup(const std::uint32_t* e, unsigned cnt, unsigned first, unsigned lane,
+                                         unsigned P, const RegFile& rf, unsigned flags, double (&acc)[ITEMS], F f) {
+    std::uint32_t ee[G];
 #pragma unroll
-        for (unsigned u = 0; u < GROUP; ++u) ee[u] = e[q + u * P];
-        double v[GROUP][NSRC][ITEMS];
+    for (unsigned u = 0; u < G; ++u) ee[u] = e[min(first + u * P + lane, cnt - 1)];
+    double v[G][NSRC][ITEMS];
 #pragma unroll
-        for (unsigned u = 0; u < GROUP; ++u)
-#pragma unroll
-            for (int s = 0; s < NSRC; ++s)
-#pragma unroll
-                for (int j = 0; j < ITEMS; ++j) v[u][s][j] = rf.at(field(ee[u], s + 1), j);
-        double r[GROUP][ITEMS];
-#pragma unroll
-        for (unsigned u = 0; u < GROUP; ++u)
-#pragma unroll
-            for (int j = 0; j < ITEMS; ++j) r[u][j] = f(v[u][0][j], v[u][NSRC > 1 ? 1 : 0][j], v[u][NSRC > 2 ? 2 : 0][j]);
-#pragma unroll
-        for (unsigned u = 0; u < GROUP; ++u)
-#pragma unroll
-            for (int j = 0; j < ITEMS; ++j) rf.at(field(ee[u], 0), j) = r[u][j];
-    }
-    for (; q < cnt; q += P) {
-        const std::uint32_t e0 = e[q];
-        double v[NSRC][ITEMS];
+    for (unsigned u = 0; u < G; ++u)
 #pragma unroll
         for (int s = 0; s < NSRC; ++s)
 #pragma unroll
-            for (int j = 0; j < ITEMS; ++j) v[s][j] = (flags & (H_A_ACC << s)) ? acc[j] : rf.at(field(e0, s + 1), j);
+            for (int j = 0; j < ITEMS; ++j)
+                v[u][s][j] = (G == 1 && (flags & (H_A_ACC << s))) ? acc[j] : rf.at(field(ee[u], s + 1), j);
+    double r[G][ITEMS];
 #pragma unroll
-        for (int j = 0; j < ITEMS; ++j) {
-            acc[j] = f(v[0][j], v[NSRC > 1 ? 1 : 0][j], v[NSRC > 2 ? 2 : 0][j]);
-            if (!(flags & H_NOSTORE)) rf.at(field(e0, 0), j) = acc[j];
-        }
+    for (unsigned u = 0; u < G; ++u)
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) r[u][j] = f(v[u][0][j], v[u][NSRC > 1 ? 1 : 0][j], v[u][NSRC > 2 ? 2 : 0][j]);
+    if (G == 1) {
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) acc[j] = r[0][j];
+        if (flags & H_NOSTORE) return;
     }
+#pragma unroll
+    for (unsigned u = 0; u < G; ++u)
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) rf.at(field(ee[u], 0), j) = r[u][j];
+}
+
+template <int ITEMS, int NSRC, unsigned GROUP, class F>
+__device__ __forceinline__ void runBundle(const std::uint32_t* e, unsigned cnt, const RegFile& rf, unsigned lane,
+                                          unsigned P, unsigned flags, double (&acc)[ITEMS], F f) {
+    const unsigned rounds = (cnt + P - 1) / P;
+    unsigned r = 0;
+    for (; r + GROUP <= rounds; r += GROUP) runGroup<ITEMS, NSRC, GROUP>(e, cnt, r * P, lane, P, rf, 0, acc, f);
+    if (GROUP > 2 && r + 2 <= rounds) {
+        runGroup<ITEMS, NSRC, 2>(e, cnt, r * P, lane, P, rf, 0, acc, f);
+        r += 2;
+    }
+    if (r < rounds) runGroup<ITEMS, NSRC, 1>(e, cnt, r * P, lane, P, rf, flags, acc, f);
 }
 
 // One entry at a time (long library sequences: keeps the code small).  Not a
@@ -242,19 +249,19 @@ __device__ bool gridBarrier(BarrierState* bar, int* hostError, unsigned long lon
 
 
 // Evaluates one tile.  A work item (one instance for one value set) is run by
-// P = A.lanes threads of one warp: warp lane l serves item slot l % (32 / P)
+// P = LANES threads of one warp: warp lane l serves item slot l % (32 / P)
 // of its warp as lane l / (32 / P), so each half-warp touches consecutive
 // slots.  Each thread serves ITEMS item slots per pass.  Shared memory holds
 // the program (when it fits) followed by the register file, laid out
 // [register][item][slot] so a warp's accesses are conflict-free.  The lanes of
 // an item split every bundle; a warp barrier after each bundle makes their
 // results visible to each other.
-template <int ITEMS, int MODE>
+template <int ITEMS, int LANES, int MODE>
 __device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t* prog, double* regs, const Tile& t,
                                          const EvalArgs& A) {
     using namespace symgb::engine;
-    const unsigned P = A.lanes;
-    const unsigned perWarp = 32u / P;
+    constexpr unsigned P = LANES;
+    constexpr unsigned perWarp = 32u / P;
     const unsigned lane = (threadIdx.x & 31u) / perWarp;
     const unsigned T = blockDim.x / P;  // item slots per block
     const unsigned me = (threadIdx.x >> 5) * perWarp + (threadIdx.x & (perWarp - 1));
@@ -354,8 +361,8 @@ __device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t
                 case OP_EXP: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_EXP>{}); break;
                 case OP_LOG: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_LOG>{}); break;
                 case OP_LDK:
-                    for (unsigned q = lane; q < cnt; q += P) {
-                        const std::uint32_t e0 = e[q];
+                    for (unsigned r = 0; r < (cnt + P - 1) / P; ++r) {  // rounds, as in runBundle
+                        const std::uint32_t e0 = e[min(r * P + lane, cnt - 1)];
                         const double c = lit[e0 >> 8];
 #pragma unroll
                         for (int j = 0; j < ITEMS; ++j) {
@@ -365,30 +372,26 @@ __device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t
                     }
                     break;
                 case OP_ST: {
+                    // Same rounds as runBundle; a lane past the end stores the
+                    // last entry's value again, to the same place.
                     const std::uint64_t yoff = k.yoff, n = k.n;
-                    unsigned q = lane;
-                    for (; q + (GROUP - 1) * P < cnt; q += GROUP * P) {
+                    const unsigned rounds = (cnt + P - 1) / P;
+                    for (unsigned r = 0; r < rounds; r += GROUP) {
                         std::uint32_t ee[GROUP];
                         double v[GROUP][ITEMS];
 #pragma unroll
-                        for (unsigned u = 0; u < GROUP; ++u) ee[u] = e[q + u * P];
-#pragma unroll
-                        for (unsigned u = 0; u < GROUP; ++u)
-#pragma unroll
-                            for (int j = 0; j < ITEMS; ++j) v[u][j] = rf.at(field(ee[u], 0), j);
+                        for (unsigned u = 0; u < GROUP; ++u) ee[u] = e[min((r + u) * P + lane, cnt - 1)];
 #pragma unroll
                         for (unsigned u = 0; u < GROUP; ++u)
 #pragma unroll
                             for (int j = 0; j < ITEMS; ++j)
-                                if (valid[j]) A.xw[(yoff + (std::uint64_t)(ee[u] >> 8) * n + ii[j]) * S + ss[j]] = v[u][j];
-                    }
-                    for (; q < cnt; q += P) {
-                        const std::uint32_t e0 = e[q];
+                                v[u][j] = (cnt == 1 && (flags & H_A_ACC)) ? acc[j] : rf.at(field(ee[u], 0), j);
 #pragma unroll
-                        for (int j = 0; j < ITEMS; ++j)
-                            if (valid[j])
-                                A.xw[(yoff + (std::uint64_t)(e0 >> 8) * n + ii[j]) * S + ss[j]] =
-                                    (flags & H_A_ACC) ? acc[j] : rf.at(field(e0, 0), j);
+                        for (unsigned u = 0; u < GROUP; ++u)
+                            if (r + u < rounds)
+#pragma unroll
+                                for (int j = 0; j < ITEMS; ++j)
+                                    if (valid[j]) A.xw[(yoff + (std::uint64_t)(ee[u] >> 8) * n + ii[j]) * S + ss[j]] = v[u][j];
                     }
                     break;
                 }
@@ -401,8 +404,15 @@ __device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t
 
 // Runs the tiles of segments [segBegin, segEnd); a grid barrier separates
 // segments (cooperative launches only when the range holds several segments).
-template <int ITEMS, int MODE>
-__global__ void evalKernel(EvalArgs A) {
+// Register cap per variant: the interpreter's occupancy is what hides the
+// latency of its shared-memory operands and FP64 results.
+template <int ITEMS>
+struct EvalRegs {
+    static constexpr int value = ITEMS == 1 ? 64 : ITEMS == 2 ? 96 : 128;
+};
+
+template <int ITEMS, int LANES, int MODE>
+__global__ void __maxnreg__(EvalRegs<ITEMS>::value) evalKernel(EvalArgs A) {
     extern __shared__ double smem[];
     std::uint64_t* progSmem = reinterpret_cast<std::uint64_t*>(smem);
     double* regs = smem + A.progCap;
@@ -425,7 +435,7 @@ __global__ void evalKernel(EvalArgs A) {
                     prog = k.prog;
                 }
             }
-            evalTile<ITEMS, MODE>(k, prog, regs, t, A);
+            evalTile<ITEMS, LANES, MODE>(k, prog, regs, t, A);
         }
         if (sg + 1 < A.segEnd)
             if (!gridBarrier(A.bar, A.hostError, A.timeoutNs)) return;

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "device.cuh"
+#include "kernels.hpp"
 #include "program.hpp"
 #include "symgb.h"
 #include "unit.hpp"
@@ -179,21 +180,8 @@ int setSmemLimit(const void* fn, std::size_t bytes) {
     return SYMGB_OK;
 }
 
-const void* evalFunction(int items, bool l2, bool lib) {
-    const int mode = (l2 ? MODE_L2 : 0) | (lib ? MODE_LIB : 0);
-#define SYMGB_EVAL_MODES(I)                                          \
-    switch (mode) {                                                 \
-        case 0: return (const void*)evalKernel<I, 0>;               \
-        case MODE_L2: return (const void*)evalKernel<I, MODE_L2>;   \
-        case MODE_LIB: return (const void*)evalKernel<I, MODE_LIB>; \
-        default: return (const void*)evalKernel<I, MODE_L2 | MODE_LIB>; \
-    }
-    switch (items) {
-        case 2: SYMGB_EVAL_MODES(2)
-        case 4: SYMGB_EVAL_MODES(4)
-        default: SYMGB_EVAL_MODES(1)
-    }
-#undef SYMGB_EVAL_MODES
+const void* evalFunction(int items, int lanes, bool l2, bool lib) {
+    return symgb::engine::evalKernelFor(items, lanes, (l2 ? MODE_L2 : 0) | (lib ? MODE_LIB : 0));
 }
 
 // Enqueues one evaluation on the unit's stream.
@@ -209,12 +197,13 @@ int enqueueRun(symgb_unit* u) {
     A.x = u->x.ptr;
     A.xw = u->x.ptr;
     A.S = (unsigned)u->numSets;
-    A.lanes = (unsigned)lanes;
+    A.reserved = 0;
     A.bar = u->barrier.ptr;
     A.hostError = u->errorDev;
     A.timeoutNs = u->barrierTimeoutNs;
     auto launch = [&](bool l2, std::uint32_t regs, std::uint32_t words, unsigned grid, bool coop) -> int {
-        const void* fn = evalFunction(items, l2, u->usesLibrary);
+        const void* fn = evalFunction(items, lanes, l2, u->usesLibrary);
+        if (!fn) return fail(SYMGB_ERR_ARGUMENT, "several lanes per item need one item per thread");
         const int bt = fitBlock(u, 0, regs, items, tpb, lanes);
         if (!bt) return fail(SYMGB_ERR_ARGUMENT, "kernel register file exceeds shared memory");
         const std::array<std::uint32_t, 6> key{(std::uint32_t)l2, regs, words, (std::uint32_t)items, (std::uint32_t)tpb,
@@ -551,6 +540,8 @@ int symgb_set_schedule(symgb_unit_t u, const symgb_schedule* s) {
     if (s->lanes_per_item != 0 && s->lanes_per_item != 1 && s->lanes_per_item != 2 && s->lanes_per_item != 4 &&
         s->lanes_per_item != 8)
         return fail(SYMGB_ERR_ARGUMENT, "lanes_per_item must be 1, 2, 4 or 8");
+    if (s->lanes_per_item > 1 && s->items_per_thread > 1)
+        return fail(SYMGB_ERR_ARGUMENT, "several lanes per item need one item per thread");
     const bool mathChanged = s->math != u->sched.math;
     u->sched = *s;
     u->dropGraph();

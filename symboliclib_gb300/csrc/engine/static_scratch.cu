@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "device.cuh"
+#include "kernels.hpp"
 #include "program.hpp"
 #include "symgb.h"
 #include "unit.hpp"
@@ -196,14 +197,8 @@ extern "C" int symgb_run_static(symgb_unit_t u, const uint32_t* index_data, cons
         while (bt >= 32 && smemFor(bt) > (std::size_t)optin) bt -= 32;
         if (bt < 32) return failStatic(SYMGB_ERR_ARGUMENT, "kernel register file exceeds shared memory");
         const std::size_t smem = smemFor(bt);
-        const void* fn;
-        if (u->usesLibrary)
-            fn = items == 4 ? (const void*)evalKernel<4, MODE_L2 | MODE_LIB>
-                            : items == 2 ? (const void*)evalKernel<2, MODE_L2 | MODE_LIB>
-                                         : (const void*)evalKernel<1, MODE_L2 | MODE_LIB>;
-        else
-            fn = items == 4 ? (const void*)evalKernel<4, MODE_L2>
-                            : items == 2 ? (const void*)evalKernel<2, MODE_L2> : (const void*)evalKernel<1, MODE_L2>;
+        const void* fn = symgb::engine::evalKernelFor(items, 1, MODE_L2 | (u->usesLibrary ? MODE_LIB : 0));
+        if (!fn) return failStatic(SYMGB_ERR_ARGUMENT, "unsupported items per thread");
         if (smem > 48 * 1024) STATIC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int perSm = 0;
         STATIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fn, bt, smem));
@@ -221,7 +216,7 @@ extern "C" int symgb_run_static(symgb_unit_t u, const uint32_t* index_data, cons
         A.xw = x;
         A.S = 1;
         A.progCap = progCap;
-        A.lanes = 1;
+        A.reserved = 0;
         A.bar = reinterpret_cast<BarrierState*>(base + oBar);
         A.hostError = reinterpret_cast<int*>(base + oBar + sizeof(BarrierState));
         A.timeoutNs = u->barrierTimeoutNs;
