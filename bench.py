@@ -38,14 +38,18 @@ FALLBACK_HBM_GBS = 6800.0
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=5000, help="timed steps (default: a timed region of about a second, "
+                                                                 "long enough for the clock samples)")
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="cotan")
     ap.add_argument("--size", type=int, default=500)
     ap.add_argument("--sets", type=int, default=1)
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--schedule", default="persistent", choices=["plain", "levels", "persistent"])
+    ap.add_argument("--schedule", default="levels", choices=["plain", "levels", "persistent"])
+    ap.add_argument("--items", type=int, default=2, help="work items per thread (1, 2, 4)")
+    ap.add_argument("--lanes", type=int, default=1, help="threads per work item (1, 2, 4, 8)")
+    ap.add_argument("--tpb", type=int, default=64, help="threads per block")
     ap.add_argument("--math", default="fast", choices=["fast", "exact"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-probe", action="store_true", help="skip the FP64 peak probe (e.g. under a profiler)")
@@ -91,6 +95,13 @@ class ClockSampler:
         reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.rows)}
+
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one step, summed
+# over the step's evalKernel launches, from one ncu capture of that exact
+# configuration on a GB300: (workload, size, sets, schedule, items, lanes,
+# threads per block) -> bytes.  Configurations not captured report null.
+MEASURED_TRAFFIC = {("cotan", 500, 1, "levels", 2, 1, 64): 82.4e6}
 
 
 def peaks():
@@ -192,7 +203,8 @@ def run_engine(args):
     u = native.Unit.from_workload(w)
     stream = torch.cuda.Stream()
     native.check(native.symgb().symgb_set_stream(u.handle, C.c_void_p(stream.cuda_stream)))
-    u.set_schedule(kind=kinds[args.schedule], math=native.MATH_FAST if args.math == "fast" else native.MATH_EXACT)
+    u.set_schedule(kind=kinds[args.schedule], math=native.MATH_FAST if args.math == "fast" else native.MATH_EXACT,
+                   threads_per_block=args.tpb, items_per_thread=args.items, lanes_per_item=args.lanes)
     u.set_num_sets(S)
     inputs = [np.tile(a, S) for a in w.inputs]
     for i, a in enumerate(inputs):
@@ -278,14 +290,18 @@ def run_engine(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh)",
             "config": workload_config(args, w, {
-                "schedule": args.schedule, "math": args.math, "l2": "flushed before every step (256 MiB write)",
+                "schedule": args.schedule, "items_per_thread": args.items, "lanes_per_item": args.lanes,
+                "threads_per_block": args.tpb, "math": args.math, "l2": "flushed before every step (256 MiB write)",
                 "front_end_s": round(front_s, 2), "kernels": int(stats.num_kernels), "levels": int(stats.num_levels),
                 "max_rel_err_vs_fp64_model": err, "plain_schedule_ms_per_step": t_plain * 1e3,
                 "plain_schedule_nnz_per_s": world * nnz * S / t_plain,
                 "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": MEASURED_TRAFFIC.get((args.workload, args.size, S, args.schedule, args.items,
+                                                          args.lanes, args.tpb)),
+                         "traffic_unit": "bytes per step (ncu capture)",
                          "algorithmic_bytes_per_step": alg_bytes},
             "fp64": {"flops_per_step": flops, "achieved_tflops": flops / t_step / 1e12,
                      "peak_tflops": fp64.value / 1e12, "peak_source": "nominal" if args.no_fp64_probe else "measured",

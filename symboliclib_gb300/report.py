@@ -135,7 +135,7 @@ def batch(args):
         u.set_num_sets(S)
         for i, a in enumerate(w.inputs):
             u.set_arg(i, np.tile(a, S))
-        tuner.Sched(args.schedule, 1, 128, 1).apply(u, graph=0)
+        tuner.Sched(args.schedule, args.items, args.tpb, 1, args.lanes).apply(u, graph=0)
     handles = (C.c_void_p * len(units))(*[u.handle.value for u, _, _ in units])
     b = C.c_void_p()
     native.check(lib.symgb_batch_create(handles, len(units), args.streams, C.byref(b)))
@@ -162,7 +162,8 @@ def batch(args):
         "instances": int(args.count), "sides": [int(sides.min()), int(sides.max())], "distinct_patterns": len(cache),
         "value_sets_total": int(sets.sum()), "output_nnz_total": int(total_nnz), "front_end_s": round(front, 1),
         "graph": {"ms": t_graph * 1e3, "nnz_per_s": total_nnz / t_graph, "kernels": int(launches),
-                  "streams": args.streams, "schedule": args.schedule},
+                  "streams": args.streams, "schedule": f"{args.schedule} items {args.items} lanes {args.lanes} "
+                                                        f"tpb {args.tpb}"},
         "plain_per_call": {"ms": plain_s * 1e3, "nnz_per_s": total_nnz / plain_s},
         "speedup": plain_s / t_graph, "max_rel_err_sampled": max(errs)}), flush=True)
 
@@ -231,12 +232,15 @@ def main():
     b.add_argument("--max-sets", type=int, default=16)
     b.add_argument("--streams", type=int, default=8)
     b.add_argument("--schedule", default="levels", choices=list(tuner.KINDS))
+    b.add_argument("--items", type=int, default=1)
+    b.add_argument("--lanes", type=int, default=2)
+    b.add_argument("--tpb", type=int, default=64)
     b.add_argument("--seed", type=int, default=7)
     b.add_argument("--steps", type=int, default=10)
     c = sub.add_parser("learned")
     c.add_argument("--target", default="neohookean")
     c.add_argument("--target-size", type=int, default=6)
-    c.add_argument("--k", type=int, default=3)
+    c.add_argument("--k", type=int, default=len(tuner.SPACE) // 15)
     c.add_argument("--epochs", type=int, default=4000)
     c.add_argument("--seed", type=int, default=5)
     args = ap.parse_args()
