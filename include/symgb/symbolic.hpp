@@ -45,8 +45,11 @@ public:
     Symbolic(OpType op, const Symbolic& c0);
     Symbolic(OpType op, const Symbolic& c0, const Symbolic& c1);
     Symbolic(OpType op, const std::vector<Symbolic>& childs);
-    // Takes ownership of `childs`, an array allocated with new Symbolic[n].
+    // Takes ownership of `childs`, an array from childArray(n).
     Symbolic(OpType op, Symbolic* childs, unsigned n);
+    // An array of n empty handles for the constructor above (pooled for
+    // short arrays).
+    static Symbolic* childArray(unsigned n);
 
     Symbolic(const Symbolic& a) : data(a.data) {
         if (data) ++data->ref;
@@ -94,6 +97,7 @@ private:
     void release();
     void finish();  // computes hash and complexity of a freshly built node
     static Node* allocate(OpType op, unsigned numChilds);
+    static void freeChildArray(Symbolic* p, unsigned n);
 };
 
 struct AlgebraicHashLess {

@@ -442,14 +442,16 @@ __global__ void __maxnreg__(EvalRegs<ITEMS>::value) evalKernel(EvalArgs A) {
     }
 }
 
-// out[s * len + j] = x[ids[j] * S + s]  (reference gatherResult, per value set)
+// out[s * len + j] = x[ids[j] * S + s]  (reference gatherResult, per value set).
+// Threads run along the output (j fastest), so the writes are contiguous; they
+// may go straight to page-locked host memory.
 __global__ void gatherKernel(const double* __restrict__ x, const std::uint32_t* __restrict__ ids, std::uint64_t len,
                              unsigned S, double* __restrict__ out) {
     const std::uint64_t w = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= len * S) return;
-    const std::uint64_t j = w / S;
-    const unsigned s = (unsigned)(w - j * S);
-    out[(std::uint64_t)s * len + j] = __ldg(x + (std::uint64_t)__ldg(ids + j) * S + s);
+    const std::uint64_t s = S == 1 ? 0 : w / len;
+    const std::uint64_t j = w - s * len;
+    out[w] = __ldg(x + (std::uint64_t)__ldg(ids + j) * S + s);
 }
 
 }  // namespace

@@ -470,9 +470,27 @@ int symgb_get_result_sets_device(symgb_unit_t u, double* d, int k) {
     return SYMGB_OK;
 }
 
+// Device-side address of a page-locked host buffer (cudaHostAlloc or
+// cudaHostRegister with mapping), or null for any other pointer.
+static double* mappedHost(double* d) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, d) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? static_cast<double*>(a.devicePointer) : nullptr;
+}
+
 int symgb_get_result_sets(symgb_unit_t u, double* d, int k) {
     if (!u || !u->initialized) return fail(SYMGB_ERR_STATE, "get_result before init");
     if (k < 0 || (std::size_t)k >= u->outStart.size() || !d) return fail(SYMGB_ERR_ARGUMENT, "bad result index");
+    // Page-locked destination: the gather writes the results there directly
+    // (one pass over the outputs instead of gather + copy).
+    if (double* dd = mappedHost(d)) {
+        if (int e = symgb_get_result_sets_device(u, dd, k)) return e;
+        SYMGB_CUDA(cudaStreamSynchronize(u->stream));
+        return checkDeviceError(u);
+    }
     const std::size_t n = u->outLength[k] * (std::size_t)u->numSets;
     if (int e = ensureOutBuf(u, n)) return e;
     if (int e = symgb_get_result_sets_device(u, u->outBuf.ptr, k)) return e;

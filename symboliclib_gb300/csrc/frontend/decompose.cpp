@@ -124,7 +124,7 @@ struct Node {
                 sortByKey(stack.end() - nc, stack.end(), [](const auto& p) { return p.second; });
             std::vector<hash_t> hashes;
             hashes.reserve(nc + 1);
-            Symbolic* kids = new Symbolic[nc];
+            Symbolic* kids = Symbolic::childArray(nc);
             Symbolic* out = kids;
             for (std::size_t i = stack.size() - nc; i < stack.size(); ++i) {
                 *out++ = std::move(stack[i].first);

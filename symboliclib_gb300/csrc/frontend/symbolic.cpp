@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cstdlib>
 #include <mutex>
+#include <new>
 
 #include "symgb/traverse.hpp"
 
@@ -54,6 +55,30 @@ NodePool& pool() {
     return p;
 }
 
+// Child arrays of up to kPooledChilds handles come from per-size free lists
+// (same ownership rules as nodes); longer arrays use new[].
+constexpr unsigned kPooledChilds = 8;
+struct ChildPool {
+    std::vector<void*> freeList[kPooledChilds + 1];
+    void* get(unsigned n) {
+        auto& f = freeList[n];
+        if (f.empty()) {
+            const std::size_t count = 2048;
+            char* slab = static_cast<char*>(std::malloc(count * n * sizeof(Symbolic)));
+            for (std::size_t i = 0; i < count; ++i) f.push_back(slab + (count - 1 - i) * n * sizeof(Symbolic));
+        }
+        void* p = f.back();
+        f.pop_back();
+        return p;
+    }
+    void put(void* p, unsigned n) { freeList[n].push_back(p); }
+};
+
+ChildPool& childPool() {
+    static thread_local ChildPool p;
+    return p;
+}
+
 }  // namespace
 
 const std::uint64_t* crc64Table() {
@@ -84,9 +109,27 @@ Symbolic::Node* Symbolic::allocate(OpType op, unsigned numChilds) {
     return n;
 }
 
+Symbolic* Symbolic::childArray(unsigned n) {
+    if (n == 0) return nullptr;
+    if (n > kPooledChilds) return new Symbolic[n];
+    Symbolic* p = static_cast<Symbolic*>(childPool().get(n));
+    for (unsigned i = 0; i < n; ++i) new (p + i) Symbolic();
+    return p;
+}
+
+void Symbolic::freeChildArray(Symbolic* p, unsigned n) {
+    if (!p) return;
+    if (n > kPooledChilds) {
+        delete[] p;
+        return;
+    }
+    for (unsigned i = 0; i < n; ++i) p[i].~Symbolic();
+    childPool().put(p, n);
+}
+
 void Symbolic::release() {
     if (data && --data->ref == 0) {
-        if (data->op != CONST && data->op != VAR && data->numChilds) delete[] data->childs;
+        if (data->op != CONST && data->op != VAR && data->numChilds) freeChildArray(data->childs, data->numChilds);
         pool().put(data);
         --g_liveNodes;
     }
@@ -107,20 +150,23 @@ Symbolic::Symbolic(int id, int group) {
 
 Symbolic::Symbolic(OpType op, const Symbolic& c0) {
     data = allocate(op, 1);
-    data->childs = new Symbolic[1]{c0};
+    data->childs = childArray(1);
+    data->childs[0] = c0;
     finish();
 }
 
 Symbolic::Symbolic(OpType op, const Symbolic& c0, const Symbolic& c1) {
     data = allocate(op, 2);
-    data->childs = new Symbolic[2]{c0, c1};
+    data->childs = childArray(2);
+    data->childs[0] = c0;
+    data->childs[1] = c1;
     finish();
 }
 
 Symbolic::Symbolic(OpType op, const std::vector<Symbolic>& childs) {
     data = allocate(op, (unsigned)childs.size());
     if (!childs.empty()) {
-        data->childs = new Symbolic[childs.size()];
+        data->childs = childArray((unsigned)childs.size());
         std::copy(childs.begin(), childs.end(), data->childs);
     }
     finish();
@@ -129,7 +175,6 @@ Symbolic::Symbolic(OpType op, const std::vector<Symbolic>& childs) {
 Symbolic::Symbolic(OpType op, Symbolic* childs, unsigned n) {
     data = allocate(op, n);
     data->childs = n ? childs : nullptr;
-    if (!n) delete[] childs;
     finish();
 }
 

@@ -143,6 +143,27 @@ def test_lanes_per_item(lanes, tpb):
         assert bits_equal(out[0], gold) and bits_equal(out[4], gold), name
 
 
+@pytest.mark.parametrize("sets", [1, 3])
+def test_results_into_page_locked_memory(sets):
+    """getResult into page-locked host memory (written by the gather kernel
+    directly) equals getResult into ordinary memory."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    _, inp, gold = load_golden("cloth", 5)
+    w = native.Workload("cloth", 5, 32)
+    u = native.Unit.from_workload(w)
+    u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_EXACT)
+    u.set_num_sets(sets)
+    for i, a in enumerate(split_inputs(w, inp)):
+        u.set_arg(i, np.tile(a, sets))
+    u.run()
+    ordinary = u.get_result(0)
+    pinned = torch.full((len(gold) * sets,), -1.0, dtype=torch.float64).pin_memory()
+    native.check(native.symgb().symgb_get_result_sets(u.handle, C.c_void_p(pinned.data_ptr()), 0))
+    assert bits_equal(pinned.numpy(), ordinary)
+    assert bits_equal(pinned.numpy()[:len(gold)], gold)
+
+
 def test_larger_cases_match_oracle():
     """Sizes beyond the fixtures: engine exact mode vs the CPU oracle."""
     for name, size, seed in [("cotan", 60, 5), ("ata", 30, 6), ("cloth", 12, 7)]:
