@@ -217,6 +217,27 @@ uint64_t symgb_algorithmic_bytes(symgb_unit_t u, int num_sets);
 int64_t symgb_kernel_program(symgb_unit_t u, int k, int math, uint64_t* words, uint64_t cap, int* registers,
                              int* num_loads);
 
+/* Versioned plan file (host only; no device needed).  Stores a plan
+ * description with its index, output-index and constant tables, so a plan
+ * built once by the front end can be reloaded without rebuilding it.  It
+ * extends the reference's raw table files indexData / constData / outIndexData
+ * (src/Utilities.hpp:156-161) with the plan metadata and templates the
+ * reference bakes into generated source, a format version and a checksum.
+ * symgb_plan_load validates the file (magic, version, byte order, checksum,
+ * sizes) and returns SYMGB_ERR_ARGUMENT for anything else; the loaded
+ * description and tables live until symgb_plan_file_free.  Errors of these
+ * calls are described by symgb_plan_last_error(). */
+typedef struct symgb_plan_file* symgb_plan_file_t;
+int symgb_plan_save(const char* path, const symgb_plan_desc* plan, const uint32_t* index_data,
+                    const uint32_t* out_index_data, const double* const_data);
+int symgb_plan_load(const char* path, symgb_plan_file_t* out);
+const symgb_plan_desc* symgb_plan_file_desc(symgb_plan_file_t f);
+const uint32_t* symgb_plan_file_index_data(symgb_plan_file_t f);
+const uint32_t* symgb_plan_file_out_index_data(symgb_plan_file_t f);
+const double* symgb_plan_file_const_data(symgb_plan_file_t f);
+void symgb_plan_file_free(symgb_plan_file_t f);
+const char* symgb_plan_last_error(void);
+
 /* Measured FP64 FMA throughput of the current device (FLOP/s, one FMA = 2). */
 int symgb_measure_fp64_rate(double* flops_per_second);
 

@@ -74,6 +74,14 @@ SYMGB_FUNCTIONS = {
     "symgb_run_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p]),
     "symgb_measure_fp64_rate": (C.c_int, [C.POINTER(C.c_double)]),
+    "symgb_plan_save": (C.c_int, [C.c_char_p, C.POINTER(PlanDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "symgb_plan_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    "symgb_plan_file_desc": (C.POINTER(PlanDesc), [C.c_void_p]),
+    "symgb_plan_file_index_data": (C.POINTER(C.c_uint32), [C.c_void_p]),
+    "symgb_plan_file_out_index_data": (C.POINTER(C.c_uint32), [C.c_void_p]),
+    "symgb_plan_file_const_data": (C.POINTER(C.c_double), [C.c_void_p]),
+    "symgb_plan_file_free": (None, [C.c_void_p]),
+    "symgb_plan_last_error": (C.c_char_p, []),
     "symgb_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "symgb_batch_run": (C.c_int, [C.c_void_p]),
     "symgb_batch_run_async": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -203,6 +211,37 @@ class Workload:
             self._lib.symgbw_free(self.handle)
         except Exception:
             pass
+
+
+def save_plan(path, plan: C.POINTER(PlanDesc), index_data, out_index_data, const_data) -> None:
+    """Writes a plan and its tables to a versioned plan file (symgb_plan_save)."""
+    lib = symgb()
+    tables = [np.ascontiguousarray(index_data, np.uint32), np.ascontiguousarray(out_index_data, np.uint32),
+              np.ascontiguousarray(const_data, np.float64)]
+    if lib.symgb_plan_save(str(path).encode(), plan, *(t.ctypes.data for t in tables)) != 0:
+        raise RuntimeError(lib.symgb_plan_last_error().decode())
+
+
+class PlanFile:
+    """A plan read back from a plan file (symgb_plan_load); the same fields as
+    a Workload's plan and tables, valid while this object lives."""
+
+    def __init__(self, path):
+        lib = symgb()
+        h = C.c_void_p()
+        if lib.symgb_plan_load(str(path).encode(), C.byref(h)) != 0:
+            raise RuntimeError(lib.symgb_plan_last_error().decode())
+        self._lib, self.handle = lib, h
+        self.plan = lib.symgb_plan_file_desc(h)
+        d = self.plan.contents
+        self.index_data = _array(lib.symgb_plan_file_index_data(h), d.num_indices, np.uint32)
+        self.out_index_data = _array(lib.symgb_plan_file_out_index_data(h), d.num_output_values, np.uint32)
+        self.const_data = _array(lib.symgb_plan_file_const_data(h), d.num_constants, np.float64)
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            self._lib.symgb_plan_file_free(self.handle)
+            self.handle = None
 
 
 class Unit:
