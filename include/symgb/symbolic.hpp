@@ -52,11 +52,11 @@ public:
     static Symbolic* childArray(unsigned n);
 
     Symbolic(const Symbolic& a) : data(a.data) {
-        if (data) ++data->ref;
+        if (data) addRef(data);
     }
     Symbolic(Symbolic&& a) noexcept : data(a.data) { a.data = nullptr; }
     Symbolic& operator=(const Symbolic& a) {
-        if (a.data) ++a.data->ref;
+        if (a.data) addRef(a.data);
         release();
         data = a.data;
         return *this;
@@ -93,7 +93,25 @@ public:
 
     hash_t computeStructureHash() const;
 
+    // Reference counts are plain integers, except inside a ConcurrentRefs
+    // scope, where several threads may copy and drop handles to shared nodes
+    // and every count update is atomic.
+    struct ConcurrentRefs {
+        ConcurrentRefs();
+        ~ConcurrentRefs();
+        ConcurrentRefs(const ConcurrentRefs&) = delete;
+        ConcurrentRefs& operator=(const ConcurrentRefs&) = delete;
+    };
+    static bool concurrentRefs() { return concurrentRefs_; }
+
 private:
+    static inline bool concurrentRefs_ = false;
+    static void addRef(Node* n) {
+        if (concurrentRefs())
+            __atomic_add_fetch(&n->ref, 1u, __ATOMIC_RELAXED);
+        else
+            ++n->ref;
+    }
     void release();
     void finish();  // computes hash and complexity of a freshly built node
     static Node* allocate(OpType op, unsigned numChilds);
@@ -104,7 +122,8 @@ struct AlgebraicHashLess {
     bool operator()(const Symbolic& a, const Symbolic& b) const { return a.ahash() < b.ahash(); }
 };
 
-// Live node count (diagnostics and leak tests).
+// Live node count (diagnostics and leak tests); exact while no other thread
+// is creating or freeing nodes.
 long long liveNodeCount();
 
 // Arithmetic with the reference's node shapes.

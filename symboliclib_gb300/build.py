@@ -33,7 +33,8 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 CXX = os.environ.get("CXX", "g++")
 CC = os.environ.get("CC", "gcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", f"-I{INCLUDE}"]
+CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-pthread", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
+            f"-I{INCLUDE}"]
 NVCCFLAGS = ARCH + ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{INCLUDE}",
                     "-Xptxas", "-warn-spills"]
 
@@ -90,12 +91,12 @@ def build(force: bool = False, verbose: bool = False) -> dict[str, Path]:
     core = [objs[s] for s in FRONTEND + ENGINE_CPP + ENGINE_CU]
     if force or _stale(libsymgb, core):
         _run([NVCC] + ARCH + ["-shared", "-o", str(libsymgb)] + [str(o) for o in core]
-             + ["-lcudart", f"-L{cudalib}", "-Xlinker", f"-rpath={cudalib}"])
+             + ["-lcudart", "-lpthread", f"-L{cudalib}", "-Xlinker", f"-rpath={cudalib}"])
     libw = LIB / "libsymgb_workloads.so"
     wobjs = [objs[s] for s in WORKLOADS]
     if force or _stale(libw, wobjs + [libsymgb]):
         _run([CXX, "-shared", "-o", str(libw)] + [str(o) for o in wobjs]
-             + [f"-L{LIB}", "-lsymgb", "-Wl,-rpath,$ORIGIN"])
+             + [f"-L{LIB}", "-lsymgb", "-lpthread", "-Wl,-rpath,$ORIGIN"])
     liboracle = ORACLE_BUILD / "liboracle.so"
     oobjs = [objs[s] for s in ORACLE_SRC]
     if force or _stale(liboracle, oobjs):

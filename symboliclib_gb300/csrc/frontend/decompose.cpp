@@ -14,6 +14,7 @@
 #include <unordered_map>
 
 #include "symgb/frontend.hpp"
+#include "symgb/parallel.hpp"
 #include "symgb/traverse.hpp"
 
 namespace symgb {
@@ -87,8 +88,14 @@ struct Node {
         complexity = (unsigned char)std::min(255, complexity + n.complexity);
     }
 
-    Symbolic extractExpression(int groupId) {
-        if (x.op() != NOOP) return x;
+    // Merged children extracted during one top-level extraction, shared within
+    // it (the same handle wherever the child occurs).
+    using MergedMemo = std::unordered_map<const Node*, std::pair<Symbolic, hash_t>>;
+
+    // This node's expression with non-merged child nodes replaced by
+    // variables of `groupId` and merged children inlined, and its structure
+    // hash.  Reads the node graph only, so blocks can be extracted in parallel.
+    std::pair<Symbolic, hash_t> extract(int groupId, MergedMemo& merged) const {
         std::vector<std::pair<Symbolic, hash_t>> stack;
         KeyMap<std::pair<Symbolic, hash_t>> cache;
 
@@ -104,8 +111,12 @@ struct Node {
             auto it = childs.find(y.ahash());
             if (it != childs.end()) {
                 if (it->second->status == MERGED) {
-                    Symbolic xpr = it->second->extractExpression(groupId);
-                    stack.emplace_back(xpr, it->second->structureHash);
+                    auto m = merged.find(it->second);
+                    if (m == merged.end()) {
+                        auto r = it->second->extract(groupId, merged);
+                        m = merged.emplace(it->second, std::move(r)).first;
+                    }
+                    stack.push_back(m->second);
                 } else {
                     stack.emplace_back(Symbolic(it->second->id, groupId), VarHash);
                 }
@@ -138,10 +149,15 @@ struct Node {
 
         prePostOrderTraverse(fullx, pre, post);
         assert(stack.size() == 1);
-        x = stack.front().first;
-        structureHash = stack.front().second;
+        return stack.front();
+    }
+
+    // Fills x (wrapped as ASSIGN to this node's variable) and structureHash.
+    void extractExpression(int groupId, MergedMemo& merged) {
+        auto r = extract(groupId, merged);
+        x = r.first;
+        structureHash = r.second;
         if (x.op() != BLOCK && x.op() != ASSIGN && status != MERGED) x = Symbolic(ASSIGN, Symbolic(id, groupId), x);
-        return x;
     }
 };
 
@@ -268,20 +284,31 @@ std::vector<ExpressionBlock> decompose(const std::vector<Symbolic>& expr, unsign
         }
     }
 
-    // 5. Blocks of the reachable, non-inlined nodes in node order.
+    // 5. Blocks of the reachable, non-inlined nodes in node order.  Each
+    // block's extraction only reads the node graph, so blocks are extracted
+    // in parallel (reference counts atomic meanwhile).
     std::vector<int> blockIdMap(nodes.size(), -1);
-    std::vector<ExpressionBlock> blocks;
+    std::vector<std::size_t> blockNode;
     for (std::size_t ni = 0; ni < nodes.size(); ++ni) {
-        if (!reachable[ni]) continue;
-        Node* x = &nodes[ni];
-        if (x->status == MERGED) continue;
-        blockIdMap[x->id] = (int)blocks.size();
-        ExpressionBlock b;
-        b.level = (int)x->level;
-        b.x = x->extractExpression(groupId);
-        b.structureHash = x->structureHash;
-        b.childs = x->allChildren();
-        blocks.push_back(std::move(b));
+        if (!reachable[ni] || nodes[ni].status == MERGED) continue;
+        blockIdMap[nodes[ni].id] = (int)blockNode.size();
+        blockNode.push_back(ni);
+    }
+    std::vector<ExpressionBlock> blocks(blockNode.size());
+    {
+        Symbolic::ConcurrentRefs concurrent;
+        parallelFor(blockNode.size(), 256, [&](std::size_t b, std::size_t e) {
+            Node::MergedMemo merged;
+            for (std::size_t i = b; i < e; ++i) {
+                Node* x = &nodes[blockNode[i]];
+                merged.clear();
+                x->extractExpression(groupId, merged);
+                blocks[i].level = (int)x->level;
+                blocks[i].x = x->x;
+                blocks[i].structureHash = x->structureHash;
+                blocks[i].childs = x->allChildren();
+            }
+        });
     }
     for (auto& b : blocks)
         for (auto& c : b.childs) c = blockIdMap[c];

@@ -7,10 +7,12 @@
 // template is then rewritten (constant folding, local common-sub-expression
 // extraction into DEFINE statements, simplification) and its statements are
 // put into dependency order.
+#include <atomic>
 #include <map>
 #include <unordered_set>
 
 #include "symgb/frontend.hpp"
+#include "symgb/parallel.hpp"
 #include "symgb/traverse.hpp"
 
 namespace symgb {
@@ -30,19 +32,41 @@ struct Lockstep {
         for (auto& s : xs) x.push_back(&s);
         init();
     }
+    // The instances are read in parallel (memory-latency bound: one pointer
+    // chase per instance); the hash is then taken in instance order.
     Lockstep(const std::vector<const Symbolic*>& parents, unsigned child) {
-        x.reserve(parents.size());
-        for (auto* p : parents) x.push_back(&(*p)[child]);
-        init();
+        x.resize(parents.size());
+        std::vector<hash_t> hs(parents.size());
+        parallelFor(parents.size(), kGrain, [&](std::size_t b, std::size_t e) {
+            for (std::size_t i = b; i < e; ++i) {
+                x[i] = &(*parents[i])[child];
+                hs[i] = x[i]->ahash();
+            }
+        });
+        if (!x.empty()) h = hashVector(hs);
     }
     // Hash of the instances' algebraic hashes (reference ComputeKernel.cpp:14-20).
     void init() {
         if (x.empty()) return;
-        std::vector<hash_t> hs;
-        hs.reserve(x.size());
-        for (auto* xi : x) hs.push_back(xi->ahash());
+        std::vector<hash_t> hs(x.size());
+        parallelFor(x.size(), kGrain, [&](std::size_t b, std::size_t e) {
+            for (std::size_t i = b; i < e; ++i) hs[i] = x[i]->ahash();
+        });
         h = hashVector(hs);
     }
+    // True if any instance differs from the first in operation or child count.
+    bool mixed() const {
+        if (x.empty()) return false;
+        const OpType op0 = x.front()->op();
+        const unsigned nc0 = x.front()->numChilds();
+        std::atomic<bool> bad{false};
+        parallelFor(x.size(), kGrain, [&](std::size_t b, std::size_t e) {
+            for (std::size_t i = b; i < e && !bad.load(std::memory_order_relaxed); ++i)
+                if (x[i]->op() != op0 || x[i]->numChilds() != nc0) bad.store(true, std::memory_order_relaxed);
+        });
+        return bad.load();
+    }
+    static constexpr std::size_t kGrain = 2048;
     unsigned numChilds() const { return x.empty() ? 0 : x.front()->numChilds(); }
     OpType op() const { return x.empty() ? NOOP : x.front()->op(); }
     bool visit() { return childCounter++ == x.front()->numChilds(); }
@@ -92,13 +116,10 @@ ComputeKernel::ComputeKernel(const std::vector<Symbolic>& instances, int simdWid
         const unsigned childPos = cur.childCounter;  // 1-based position of this child
         // Every instance must have the same operation and child count here
         // (the reference asserts this, ComputeKernel.cpp:166).
-        for (const Symbolic* xi : cur.x)
-            if (xi->op() != parentOp || xi->numChilds() != cur.numChilds())
-                throw GroupMismatch("kernel group holds structurally different blocks");
+        if (childPos == 1 && cur.mixed()) throw GroupMismatch("kernel group holds structurally different blocks");
         Lockstep data(cur.x, childPos - 1);
-        if (data.op() == VAR || data.op() == CONST)  // leaf lists are never visited as `cur`
-            for (const Symbolic* xi : data.x)
-                if (xi->op() != data.op()) throw GroupMismatch("kernel group holds structurally different blocks");
+        if ((data.op() == VAR || data.op() == CONST) && data.mixed())  // leaf lists are never visited as `cur`
+            throw GroupMismatch("kernel group holds structurally different blocks");
         auto it = seen.find(data.h);
         if (it != seen.end()) {
             built.push_back(it->second);

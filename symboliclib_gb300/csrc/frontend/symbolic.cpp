@@ -27,7 +27,26 @@ struct Crc64Table {
     }
 };
 
-std::atomic<long long> g_liveNodes{0};
+// Live node count: one counter per thread (a single shared atomic would be
+// contended by every allocation of the parallel front-end passes), summed on
+// demand.  Counters are never freed, so a thread's net count survives it.
+struct LiveCounters {
+    std::mutex m;
+    std::vector<long long*> all;
+};
+LiveCounters& liveCounters() {
+    static LiveCounters* c = new LiveCounters();
+    return *c;
+}
+long long& liveNodes() {
+    static thread_local long long* mine = [] {
+        auto* p = new long long(0);
+        std::lock_guard<std::mutex> g(liveCounters().m);
+        liveCounters().all.push_back(p);
+        return p;
+    }();
+    return *mine;
+}
 
 // Nodes are small and created by the million; a per-thread free list keeps
 // allocation off the general-purpose heap.
@@ -86,7 +105,12 @@ const std::uint64_t* crc64Table() {
     return table.t;
 }
 
-long long liveNodeCount() { return g_liveNodes.load(); }
+long long liveNodeCount() {
+    std::lock_guard<std::mutex> g(liveCounters().m);
+    long long n = 0;
+    for (long long* p : liveCounters().all) n += __atomic_load_n(p, __ATOMIC_RELAXED);
+    return n;
+}
 
 int& Symbolic::uniqueVariableCounter() {
     static int counter = 0;
@@ -105,7 +129,7 @@ Symbolic::Node* Symbolic::allocate(OpType op, unsigned numChilds) {
     n->numChilds = numChilds;
     n->algebraicHash = 0;
     n->childs = nullptr;
-    ++g_liveNodes;
+    ++liveNodes();
     return n;
 }
 
@@ -127,11 +151,16 @@ void Symbolic::freeChildArray(Symbolic* p, unsigned n) {
     childPool().put(p, n);
 }
 
+Symbolic::ConcurrentRefs::ConcurrentRefs() { concurrentRefs_ = true; }
+Symbolic::ConcurrentRefs::~ConcurrentRefs() { concurrentRefs_ = false; }
+
 void Symbolic::release() {
-    if (data && --data->ref == 0) {
+    if (!data) return;
+    const bool last = concurrentRefs() ? __atomic_sub_fetch(&data->ref, 1u, __ATOMIC_ACQ_REL) == 0 : --data->ref == 0;
+    if (last) {
         if (data->op != CONST && data->op != VAR && data->numChilds) freeChildArray(data->childs, data->numChilds);
         pool().put(data);
-        --g_liveNodes;
+        --liveNodes();
     }
     data = nullptr;
 }
