@@ -1,0 +1,31 @@
+"""The front end's parallel passes (lockstep walk over kernel instances, block
+extraction) give the same plan as running them on one thread."""
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+SCRIPT = r"""
+import hashlib, sys
+sys.path.insert(0, sys.argv[1])
+from symboliclib_gb300 import native
+for c in [("cloth", 14, 7), ("cotan", 40, 5), ("neohookean", 3, 9), ("random", 20000, 22), ("random", 20000, 28)]:
+    w = native.Workload(*c, text=True)
+    print(c, hashlib.sha1(w.plan_text.encode()).hexdigest())
+"""
+
+
+def plan_hashes(threads: int) -> str:
+    env = dict(os.environ, SYMGB_THREADS=str(threads))
+    r = subprocess.run([sys.executable, "-c", SCRIPT, str(ROOT)], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return r.stdout
+
+
+def test_parallel_front_end_matches_serial():
+    serial = plan_hashes(1)
+    assert serial.count("\n") == 5
+    assert plan_hashes(4) == serial
+    assert plan_hashes(13) == serial
