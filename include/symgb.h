@@ -102,7 +102,9 @@ typedef struct symgb_schedule {
     int32_t math;               /* SYMGB_MATH_* */
     int32_t threads_per_block;  /* 0 = plan default */
     int32_t items_per_tile;     /* work items per CTA tile in fused schedules (0 = auto) */
-    int32_t blocks_per_sm;      /* persistent grid: CTAs per SM (0 = occupancy maximum) */
+    int32_t blocks_per_sm;      /* CTAs per SM.  Persistent: 0 = occupancy maximum.  Plain and
+                                   levels: 0 = one CTA per tile, > 0 caps the grid at this many
+                                   CTAs per SM, each taking several tiles */
     int32_t use_graph;          /* capture run() into a CUDA graph and replay it */
     int32_t items_per_thread;   /* work items per thread per pass: 1, 2 or 4 (0 = 1) */
     int32_t fusion_depth;       /* LEVELS: consecutive levels per launch (0/1 = one level; a

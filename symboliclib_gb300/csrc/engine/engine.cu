@@ -227,6 +227,10 @@ int enqueueRun(symgb_unit* u) {
             void* args[] = {(void*)&A};
             SYMGB_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(bt), args, smem, u->stream));
         } else {
+            // A CTA loops over tiles; capping the grid makes each CTA take
+            // several tiles (fewer CTA launches, one program staging per CTA).
+            if (u->sched.blocks_per_sm > 0)
+                grid = std::max(1u, std::min<unsigned>(grid, (unsigned)(u->sched.blocks_per_sm * u->smCount)));
             void* args[] = {(void*)&A};
             SYMGB_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(bt), args, smem, u->stream));
         }
