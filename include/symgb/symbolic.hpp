@@ -102,10 +102,10 @@ public:
         ConcurrentRefs(const ConcurrentRefs&) = delete;
         ConcurrentRefs& operator=(const ConcurrentRefs&) = delete;
     };
-    static bool concurrentRefs() { return concurrentRefs_; }
+    static bool concurrentRefs() { return __atomic_load_n(&concurrentScopes_, __ATOMIC_RELAXED) != 0; }
 
 private:
-    static inline bool concurrentRefs_ = false;
+    static inline int concurrentScopes_ = 0;  // open ConcurrentRefs scopes, any thread
     static void addRef(Node* n) {
         if (concurrentRefs())
             __atomic_add_fetch(&n->ref, 1u, __ATOMIC_RELAXED);

@@ -151,8 +151,8 @@ void Symbolic::freeChildArray(Symbolic* p, unsigned n) {
     childPool().put(p, n);
 }
 
-Symbolic::ConcurrentRefs::ConcurrentRefs() { concurrentRefs_ = true; }
-Symbolic::ConcurrentRefs::~ConcurrentRefs() { concurrentRefs_ = false; }
+Symbolic::ConcurrentRefs::ConcurrentRefs() { __atomic_add_fetch(&concurrentScopes_, 1, __ATOMIC_SEQ_CST); }
+Symbolic::ConcurrentRefs::~ConcurrentRefs() { __atomic_sub_fetch(&concurrentScopes_, 1, __ATOMIC_SEQ_CST); }
 
 void Symbolic::release() {
     if (!data) return;
