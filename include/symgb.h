@@ -114,6 +114,20 @@ typedef struct symgb_schedule {
                                    register file, which divides its shared memory per thread */
 } symgb_schedule;
 
+/* Launch shape of one kernel (items per thread, lanes per item, threads per
+ * block; 0 = the schedule's value).  Used by the plain schedule for that
+ * kernel's launch, and by the levels schedule for a level whose largest kernel
+ * it is.  Changes no value. */
+int symgb_set_kernel_shape(symgb_unit_t u, int k, int items_per_thread, int lanes_per_item, int threads_per_block);
+
+/* Per-kernel timing for the autotuner: runs the plain schedule (one launch per
+ * kernel, in execution order, with the kernels' shapes) `reps` times on the
+ * unit's stream, writing the mean microseconds of each kernel's launch into
+ * us_per_kernel[num_kernels].  With flush != NULL, flush_bytes of that device
+ * buffer are overwritten before every repetition (L2 eviction).  The x slots
+ * are written as by symgb_run. */
+int symgb_time_kernels(symgb_unit_t u, int reps, void* flush, uint64_t flush_bytes, double* us_per_kernel);
+
 /* --- the reference's generated-library calls, per unit ----------------------- */
 
 /* Creates a unit from a plan description (copies it) and compiles the templates

@@ -115,7 +115,9 @@ int uploadPrograms(symgb_unit* u) {
 int buildTiles(symgb_unit* u) {
     const int S = u->numSets;
     const int items = u->sched.items_per_tile > 0 ? u->sched.items_per_tile : u->launchTpb() / u->lanes() * u->items();
-    if (u->tilesSets == S && u->tilesItems == items && u->tilesMath == u->mathIndex()) return SYMGB_OK;
+    if (u->tilesSets == S && u->tilesItems == items && u->tilesMath == u->mathIndex() &&
+        u->tilesShapes == u->shapesVersion)
+        return SYMGB_OK;
     u->hostTiles.clear();
     u->hostLevelSeg.assign(1, 0);
     u->hostKernelSeg.assign(1, 0);
@@ -124,8 +126,13 @@ int buildTiles(symgb_unit* u) {
             if (u->kernels[k].desc.level != L) continue;
             const std::uint64_t total = u->kernels[k].desc.num_instances * (std::uint64_t)S;
             if (!total) continue;
-            for (std::uint64_t st = 0; st < total; st += items)
-                u->hostTiles.push_back({(std::uint32_t)k, (std::uint32_t)std::min<std::uint64_t>(items, total - st), st});
+            // One pass of the kernel's launch shape per tile (unless the
+            // schedule fixes the tile size).
+            const symgb_unit::Shape sh = u->shapeOf(k);
+            const std::uint64_t tile = u->sched.items_per_tile > 0 ? (std::uint64_t)u->sched.items_per_tile
+                                                                   : (std::uint64_t)(sh.tpb / sh.lanes * sh.items);
+            for (std::uint64_t st = 0; st < total; st += tile)
+                u->hostTiles.push_back({(std::uint32_t)k, (std::uint32_t)std::min<std::uint64_t>(tile, total - st), st});
             u->hostKernelSeg.push_back((std::uint32_t)u->hostTiles.size());
         }
         u->hostLevelSeg.push_back((std::uint32_t)u->hostTiles.size());
@@ -139,6 +146,7 @@ int buildTiles(symgb_unit* u) {
     SYMGB_CUDA(cudaMemcpy(u->kernelSeg.ptr, u->hostKernelSeg.data(), u->hostKernelSeg.size() * 4, cudaMemcpyHostToDevice));
     u->tilesSets = S;
     u->tilesItems = items;
+    u->tilesShapes = u->shapesVersion;
     u->tilesMath = u->mathIndex();
     return SYMGB_OK;
 }
@@ -184,8 +192,10 @@ const void* evalFunction(int items, int lanes, bool l2, bool lib) {
     return symgb::engine::evalKernelFor(items, lanes, (l2 ? MODE_L2 : 0) | (lib ? MODE_LIB : 0));
 }
 
-// Enqueues one evaluation on the unit's stream.
-int enqueueRun(symgb_unit* u) {
+// Enqueues one evaluation on the unit's stream.  With `kernelEvents`, runs the
+// plain schedule whatever the unit's and records an event before and after
+// each kernel's launch (per-kernel timing).
+int enqueueRun(symgb_unit* u, const std::vector<cudaEvent_t>* kernelEvents = nullptr) {
     if (int e = buildTiles(u)) return e;
     const int items = u->items();
     const int tpb = u->launchTpb();
@@ -201,7 +211,9 @@ int enqueueRun(symgb_unit* u) {
     A.bar = u->barrier.ptr;
     A.hostError = u->errorDev;
     A.timeoutNs = u->barrierTimeoutNs;
-    auto launch = [&](bool l2, std::uint32_t regs, std::uint32_t words, unsigned grid, bool coop) -> int {
+    auto launch = [&](bool l2, std::uint32_t regs, std::uint32_t words, unsigned grid, bool coop,
+                      symgb_unit::Shape sh) -> int {
+        const int items = sh.items, lanes = sh.lanes, tpb = sh.tpb;
         const void* fn = evalFunction(items, lanes, l2, u->usesLibrary);
         if (!fn) return fail(SYMGB_ERR_ARGUMENT, "several lanes per item need one item per thread");
         const int bt = fitBlock(u, 0, regs, items, tpb, lanes);
@@ -237,7 +249,8 @@ int enqueueRun(symgb_unit* u) {
         ++launches;
         return SYMGB_OK;
     };
-    switch (u->sched.kind) {
+    const symgb_unit::Shape unitShape{items, lanes, tpb};
+    switch (kernelEvents ? SYMGB_SCHEDULE_PLAIN : u->sched.kind) {
         case SYMGB_SCHEDULE_PLAIN: {
             A.segments = u->kernelSeg.ptr;
             for (std::size_t sgi = 0; sgi + 1 < u->hostKernelSeg.size(); ++sgi) {
@@ -245,7 +258,11 @@ int enqueueRun(symgb_unit* u) {
                 const std::uint32_t k = u->hostTiles[u->hostKernelSeg[sgi]].kernel;
                 A.segBegin = (int)sgi;
                 A.segEnd = (int)sgi + 1;
-                if (int e = launch(false, u->hostDevKernels[k].regs, u->hostDevKernels[k].nwords, nt, false)) return e;
+                if (kernelEvents) SYMGB_CUDA(cudaEventRecord((*kernelEvents)[2 * k], u->stream));
+                if (int e = launch(false, u->hostDevKernels[k].regs, u->hostDevKernels[k].nwords, nt, false,
+                                   u->shapeOf(k)))
+                    return e;
+                if (kernelEvents) SYMGB_CUDA(cudaEventRecord((*kernelEvents)[2 * k + 1], u->stream));
             }
             break;
         }
@@ -265,7 +282,21 @@ int enqueueRun(symgb_unit* u) {
                 if (!maxTiles) continue;
                 A.segBegin = L;
                 A.segEnd = L1;
-                if (int e = launch(L1 - L > 1, regs, words, maxTiles, L1 - L > 1)) return e;
+                // A single level runs in the launch shape of its largest kernel.
+                symgb_unit::Shape sh = unitShape;
+                if (L1 - L == 1) {
+                    double most = -1;
+                    for (std::size_t k = 0; k < u->kernels.size(); ++k) {
+                        if (u->kernels[k].desc.level != L) continue;
+                        const double work = (double)u->kernels[k].desc.num_instances *
+                                            (double)(u->kernels[k].prog[u->mathIndex()].operations + 1);
+                        if (work > most) {
+                            most = work;
+                            sh = u->shapeOf(k);
+                        }
+                    }
+                }
+                if (int e = launch(L1 - L > 1, regs, words, maxTiles, L1 - L > 1, sh)) return e;
             }
             break;
         }
@@ -276,7 +307,7 @@ int enqueueRun(symgb_unit* u) {
             std::uint32_t maxTiles = 1;
             for (int L = 0; L < u->numLevels; ++L)
                 maxTiles = std::max(maxTiles, u->hostLevelSeg[L + 1] - u->hostLevelSeg[L]);
-            if (int e = launch(true, maxRegs(u), maxWords(u), maxTiles, true)) return e;
+            if (int e = launch(true, maxRegs(u), maxWords(u), maxTiles, true, unitShape)) return e;
             break;
         }
         default: return fail(SYMGB_ERR_ARGUMENT, "unknown schedule kind");
@@ -570,6 +601,57 @@ int symgb_set_schedule(symgb_unit_t u, const symgb_schedule* s) {
     u->tilesSets = -1;
     if (mathChanged && u->initialized) return uploadPrograms(u);
     return SYMGB_OK;
+}
+
+int symgb_set_kernel_shape(symgb_unit_t u, int k, int items_per_thread, int lanes_per_item, int threads_per_block) {
+    if (!u) return fail(SYMGB_ERR_ARGUMENT, "null unit");
+    if (k < 0 || (std::size_t)k >= u->kernels.size()) return fail(SYMGB_ERR_ARGUMENT, "bad kernel index");
+    if (items_per_thread != 0 && items_per_thread != 1 && items_per_thread != 2 && items_per_thread != 4)
+        return fail(SYMGB_ERR_ARGUMENT, "items_per_thread must be 0, 1, 2 or 4");
+    if (lanes_per_item != 0 && lanes_per_item != 1 && lanes_per_item != 2 && lanes_per_item != 4 && lanes_per_item != 8)
+        return fail(SYMGB_ERR_ARGUMENT, "lanes_per_item must be 0, 1, 2, 4 or 8");
+    if (lanes_per_item > 1 && items_per_thread > 1)
+        return fail(SYMGB_ERR_ARGUMENT, "several lanes per item need one item per thread");
+    if (threads_per_block < 0 || threads_per_block > 1024 || (threads_per_block % 32))
+        return fail(SYMGB_ERR_ARGUMENT, "threads_per_block must be a multiple of 32 up to 1024");
+    u->kernelShape.resize(u->kernels.size(), symgb_unit::Shape{0, 0, 0});
+    u->kernelShape[k] = symgb_unit::Shape{items_per_thread, lanes_per_item, threads_per_block};
+    ++u->shapesVersion;
+    u->dropGraph();
+    return SYMGB_OK;
+}
+
+int symgb_time_kernels(symgb_unit_t u, int reps, void* flush, uint64_t flush_bytes, double* us_per_kernel) {
+    if (!u || !us_per_kernel || reps < 1) return fail(SYMGB_ERR_ARGUMENT, "bad argument");
+    if (!u->initialized) return fail(SYMGB_ERR_STATE, "time_kernels before init");
+    if (int e = buildTiles(u)) return e;
+    const std::size_t nk = u->kernels.size();
+    const std::size_t per = 2 * nk;
+    while (u->timingEvents.size() < per * (std::size_t)reps) {
+        cudaEvent_t ev;
+        SYMGB_CUDA(cudaEventCreate(&ev));
+        u->timingEvents.push_back(ev);
+    }
+    for (std::size_t k = 0; k < nk; ++k) us_per_kernel[k] = 0.0;
+    for (int r = 0; r < reps; ++r) {
+        if (flush && flush_bytes) SYMGB_CUDA(cudaMemsetAsync(flush, r & 0xff, flush_bytes, u->stream));
+        const std::vector<cudaEvent_t> evs(u->timingEvents.begin() + per * r, u->timingEvents.begin() + per * (r + 1));
+        // kernels without work are not launched: their two events are recorded back to back
+        for (std::size_t k = 0; k < nk; ++k)
+            if (!u->kernels[k].desc.num_instances) {
+                SYMGB_CUDA(cudaEventRecord(evs[2 * k], u->stream));
+                SYMGB_CUDA(cudaEventRecord(evs[2 * k + 1], u->stream));
+            }
+        if (int e = enqueueRun(u, &evs)) return e;
+    }
+    SYMGB_CUDA(cudaStreamSynchronize(u->stream));
+    for (int r = 0; r < reps; ++r)
+        for (std::size_t k = 0; k < nk; ++k) {
+            float ms = 0.f;
+            SYMGB_CUDA(cudaEventElapsedTime(&ms, u->timingEvents[per * r + 2 * k], u->timingEvents[per * r + 2 * k + 1]));
+            us_per_kernel[k] += ms * 1e3 / reps;
+        }
+    return checkDeviceError(u);
 }
 
 int symgb_get_schedule(symgb_unit_t u, symgb_schedule* s) {

@@ -104,6 +104,8 @@ struct symgb_unit {
 
     void release() {
         dropGraph();
+        for (cudaEvent_t e : timingEvents) cudaEventDestroy(e);
+        timingEvents.clear();
         x.reset();
         c.reset();
         staging.reset();
@@ -131,5 +133,26 @@ struct symgb_unit {
     int lanes() const { return sched.lanes_per_item > 1 ? sched.lanes_per_item : 1; }
     // Block size of a launch: whole warps when several lanes share an item.
     int launchTpb() const { return lanes() > 1 ? std::max(32, tpb() / 32 * 32) : tpb(); }
+
+    // Per-kernel launch shape (symgb_set_kernel_shape); zeros take the schedule's.
+    struct Shape {
+        int items, lanes, tpb;
+    };
+    std::vector<Shape> kernelShape;
+    int shapesVersion = 0, tilesShapes = -1;
+    std::vector<cudaEvent_t> timingEvents;
+    Shape shapeOf(std::size_t k) const {
+        Shape s{items(), lanes(), tpb()};
+        if (k < kernelShape.size()) {
+            const Shape& o = kernelShape[k];
+            if (o.items || o.lanes || o.tpb) {
+                s.items = o.items ? o.items : 1;
+                s.lanes = o.lanes ? o.lanes : 1;
+                if (o.tpb) s.tpb = o.tpb;
+            }
+        }
+        if (s.lanes > 1) s.tpb = std::max(32, s.tpb / 32 * 32);
+        return s;
+    }
 };
 

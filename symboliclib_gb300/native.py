@@ -74,6 +74,8 @@ SYMGB_FUNCTIONS = {
     "symgb_run_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p]),
     "symgb_measure_fp64_rate": (C.c_int, [C.POINTER(C.c_double)]),
+    "symgb_set_kernel_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "symgb_time_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_double)]),
     "symgb_plan_save": (C.c_int, [C.c_char_p, C.POINTER(PlanDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
     "symgb_plan_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
     "symgb_plan_file_desc": (C.POINTER(PlanDesc), [C.c_void_p]),
@@ -256,6 +258,8 @@ class Unit:
                         np.ascontiguousarray(const_data, np.float64))
         check(lib.symgb_init(h, *(t.ctypes.data for t in self._tables)))
         d = plan.contents
+        self.kernel_instances = [int(d.kernels[k].num_instances) for k in range(d.num_kernels)]
+        self.kernel_levels = [int(d.kernels[k].level) for k in range(d.num_kernels)]
         self.arg_length = [int(d.arg_length[i]) for i in range(d.num_args)]
         self.output_length = [int(d.output_length[i]) for i in range(d.num_outputs)]
 
@@ -271,6 +275,22 @@ class Unit:
 
     def set_num_sets(self, n: int) -> None:
         check(self._lib.symgb_set_num_sets(self.handle, n))
+
+    @property
+    def num_kernels(self) -> int:
+        return len(self.kernel_instances)
+
+    def set_kernel_shape(self, k: int, items: int = 0, lanes: int = 0, tpb: int = 0) -> None:
+        check(self._lib.symgb_set_kernel_shape(self.handle, k, items, lanes, tpb))
+
+    def time_kernels(self, reps: int = 5, flush=None) -> np.ndarray:
+        """Mean microseconds per kernel launch under the plain schedule
+        (flush: a torch CUDA tensor overwritten before every repetition)."""
+        out = (C.c_double * self.num_kernels)()
+        ptr = C.c_void_p(flush.data_ptr()) if flush is not None else None
+        nbytes = flush.numel() * flush.element_size() if flush is not None else 0
+        check(self._lib.symgb_time_kernels(self.handle, reps, ptr, nbytes, out))
+        return np.array(out[:])
 
     @property
     def num_sets(self) -> int:

@@ -11,6 +11,10 @@
         the MLP cost model trained on tuner timings of other workloads, then
         used to pick the target's schedule: regret and tuning time against
         exhaustive search.
+    python -m symboliclib_gb300.report kernels --target cloth --target-size 100 --sets 16
+        per-kernel launch shapes: the kernel-level MLP (trained on other
+        units' per-kernel timings) against exhaustive per-kernel tuning, and
+        the tuned runs against the best unit-wide schedule.
 Each prints one JSON line.  Errors are measured against the workload's FP64
 model evaluated in double (floor 1e-4 of the largest magnitude).
 """
@@ -77,9 +81,20 @@ def single(args):
     space = tuner.SPACE if args.full_space else [s for s in tuner.SPACE if s.tile == 1]
     tt = time.perf_counter()
     res = tuner.exhaustive(u, stream, flush, space=space, runs=max(3, args.steps // 2))
-    tune_s = time.perf_counter() - tt
     t_batch = tuner.time_schedule(u, res.best, stream, flush, runs=args.steps) * 1e-6
-    res.best.apply(u)
+    # per-kernel launch shapes on the plain schedule, kept if faster
+    pk = tuner.tune_kernels(u, flush, reps=max(3, args.steps // 2))
+    plain_any = tuner.Sched("plain", 1, 128, 1)
+    t_pk = tuner.time_schedule(u, plain_any, stream, flush, runs=args.steps) * 1e-6
+    tune_s = time.perf_counter() - tt
+    chosen = f"{res.best}"
+    if t_pk < t_batch:
+        t_batch, chosen = t_pk, f"plain with per-kernel shapes {[list(x) for x in pk.shapes]}"
+        plain_any.apply(u)
+    else:
+        for k in range(u.num_kernels):
+            u.set_kernel_shape(k)
+        res.best.apply(u)
     u.run()
     out = u.get_result(0).reshape(S, -1)
     err_batch = max(rel_err(out[s], w.numeric) for s in (0, S - 1))
@@ -93,10 +108,11 @@ def single(args):
         "kernels": int(st.num_kernels), "levels": int(st.num_levels), "max_registers": int(st.max_registers),
         "plain": {"ms_per_execute": t_plain * 1e3, "nnz_per_s": nnz / t_plain, "max_rel_err": err_plain,
                   "hbm_gbs": u.algorithmic_bytes(1) / t_plain / 1e9},
-        "batched": {"schedule": str(res.best), "ms_per_execute": t_batch * 1e3, "nnz_per_s": nnz * S / t_batch,
+        "batched": {"schedule": chosen, "unit_wide_best": str(res.best), "unit_wide_ms": res.best_us * 1e-3,
+                    "per_kernel_plain_ms": t_pk * 1e3, "ms_per_execute": t_batch * 1e3, "nnz_per_s": nnz * S / t_batch,
                     "max_rel_err": err_batch, "algorithmic_bytes": alg, "hbm_gbs": alg / t_batch / 1e9,
                     "hbm_frac": alg / t_batch / 1e9 / peak, "fp64_tflops": flops / t_batch / 1e12,
-                    "fp64_frac": flops / t_batch / fp, "tuning_s": round(tune_s, 1), "schedules_timed": res.timed},
+                    "fp64_frac": flops / t_batch / fp, "tuning_s": round(tune_s, 1), "schedules_timed": res.timed + pk.timed},
         "speedup_batched_vs_plain": (nnz * S / t_batch) / (nnz / t_plain),
         "hbm_peak_gbs": peak, "fp64_peak_tflops": fp / 1e12}), flush=True)
 
@@ -215,6 +231,65 @@ def learned(args):
         "timings_ratio": full.timed / max(1, prop.timed)}), flush=True)
 
 
+def kernels(args):
+    """Per-kernel launch shapes: exhaustive per-kernel tuning against the
+    learned per-kernel proposer (trained on other units' kernel timings), and
+    the tuned plain / levels runs against the best unit-wide schedule."""
+    flush = flush_buffer()
+    train = [("cotan", s, 1 + s, S) for s in (60, 120, 200) for S in (1, 8)] + \
+            [("cloth", s, 2 + s, S) for s in (12, 20, 30) for S in (1, 8)] + \
+            [("ata", s, 3 + s, 1) for s in (40, 70)] + [("random", n, 10 + k, 1) for k, n in
+                                                       enumerate([20000, 40000, 60000, 90000] * 3)]
+    X, y = [], []
+    t_collect = time.perf_counter()
+    for name, size, seed, S in train:
+        w = native.Workload(name, size, seed)
+        u = native.Unit.from_workload(w)
+        u.set_num_sets(S)
+        for i, a in enumerate(w.inputs):
+            u.set_arg(i, np.tile(a, S))
+        tuner.bind_stream(u)
+        res = tuner.tune_kernels(u, flush, reps=3)
+        sums = [tuner.program_summary(u, k) for k in range(u.num_kernels)]
+        for sh, t in res.table.items():
+            for k in range(u.num_kernels):
+                if u.kernel_instances[k] and t[k] > 0:
+                    X.append(tuner.kernel_features(u, k, S, sh, sums[k]))
+                    y.append(t[k])
+    t_collect = time.perf_counter() - t_collect
+    model = tuner.KernelCostModel(seed=args.seed)
+    loss = model.fit(np.stack(X), np.array(y), epochs=args.epochs)
+
+    w = native.Workload(args.target, args.target_size, args.seed)
+    S = args.sets
+    u = native.Unit.from_workload(w)
+    u.set_num_sets(S)
+    for i, a in enumerate(w.inputs):
+        u.set_arg(i, np.tile(a, S))
+    stream = tuner.bind_stream(u)
+    unitwide = tuner.exhaustive(u, stream, flush, runs=5)
+    full = tuner.tune_kernels(u, flush, reps=5)
+    plain_tuned = tuner.time_schedule(u, tuner.Sched("plain", 1, 128, 1), stream, flush, runs=7)
+    levels_tuned = tuner.time_schedule(u, tuner.Sched("levels", 1, 128, 1), stream, flush, runs=7)
+    learned = tuner.tune_kernels_with_model(u, model, S, flush, k_top=args.k, reps=5)
+    learned_total = float(sum(full.table[sh][k] for k, sh in enumerate(learned.shapes) if sh in full.table))
+    u.run()
+    err = rel_err(u.get_result(0).reshape(S, -1)[S - 1], w.numeric)
+    print(json.dumps({
+        "target": f"{args.target} {args.target_size}", "value_sets": S, "kernels": u.num_kernels,
+        "training_samples": len(y), "training_units": len(train), "collect_s": round(t_collect, 1),
+        "fit_mse_log": loss,
+        "unit_wide_best": {"schedule": str(unitwide.best), "us": unitwide.best_us},
+        "per_kernel_exhaustive": {"sum_of_kernels_us": full.total_us, "plain_run_us": plain_tuned,
+                                  "levels_run_us": levels_tuned, "passes": full.timed, "seconds": full.seconds,
+                                  "shapes": [list(s) for s in full.shapes]},
+        "per_kernel_learned": {"sum_of_kernels_us": learned_total, "passes": learned.timed, "seconds": learned.seconds,
+                               "k": args.k},
+        "regret": learned_total / full.total_us - 1.0,
+        "tuning_time_ratio": full.seconds / max(learned.seconds, 1e-9),
+        "max_rel_err": err}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -243,8 +318,15 @@ def main():
     c.add_argument("--k", type=int, default=len(tuner.SPACE) // 15)
     c.add_argument("--epochs", type=int, default=4000)
     c.add_argument("--seed", type=int, default=5)
+    d = sub.add_parser("kernels")
+    d.add_argument("--target", default="cloth")
+    d.add_argument("--target-size", type=int, default=100)
+    d.add_argument("--sets", type=int, default=16)
+    d.add_argument("--k", type=int, default=2)
+    d.add_argument("--epochs", type=int, default=4000)
+    d.add_argument("--seed", type=int, default=5)
     args = ap.parse_args()
-    {"single": single, "batch": batch, "learned": learned}[args.cmd](args)
+    {"single": single, "batch": batch, "learned": learned, "kernels": kernels}[args.cmd](args)
 
 
 if __name__ == "__main__":

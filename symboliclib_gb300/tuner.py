@@ -159,3 +159,125 @@ def tune_with_model(unit: native.Unit, model: CostModel, stream, flush=None, k: 
             continue
     best = min(timings, key=timings.get)
     return TuneResult(best, timings[best], timings, time.perf_counter() - t0, len(timings))
+
+
+# ------------------------------------------------------- per-kernel shapes
+
+# Launch shapes a single kernel can take: (items per thread, lanes per item)
+# x threads per block.
+KERNEL_SHAPES = [(i, l, t) for (i, l) in SHAPES for t in (64, 128, 256)]
+
+_OPNAMES = {5: "add", 6: "sub", 7: "mul", 8: "div", 9: "neg", 10: "sqrt", 11: "rec", 12: "fma", 23: "fma", 24: "fma",
+            25: "fma"}
+
+
+def program_summary(unit: native.Unit, k: int, math_mode: int = native.MATH_FAST) -> dict:
+    """Operation counts of kernel k's device program (decoded bundles)."""
+    lib = native.symgb()
+    r, nl = C.c_int(), C.c_int()
+    n = lib.symgb_kernel_program(unit.handle, k, math_mode, None, 0, C.byref(r), C.byref(nl))
+    buf = (C.c_uint64 * n)()
+    lib.symgb_kernel_program(unit.handle, k, math_mode, buf, n, C.byref(r), C.byref(nl))
+    words = list(buf)
+    pc, bundles, entries = nl.value, 0, 0
+    counts = {"add": 0, "sub": 0, "mul": 0, "div": 0, "neg": 0, "sqrt": 0, "rec": 0, "fma": 0, "st": 0, "other": 0}
+    while words[pc] & 0xff:
+        op, cnt = words[pc] & 0xff, (words[pc] >> 8) & 0xffff
+        counts["st" if op == 4 else _OPNAMES.get(op, "other")] += cnt
+        bundles += 1
+        entries += cnt
+        pc += 1 + (cnt + 1) // 2
+    return {"registers": r.value, "loads": nl.value, "bundles": bundles, "entries": entries, **counts}
+
+
+def kernel_features(unit: native.Unit, k: int, num_sets: int, shape, summary: dict) -> np.ndarray:
+    """Tree features of one kernel (its template program) and a launch shape."""
+    items, lanes, tpb = shape
+    lg = lambda v: math.log1p(float(v))
+    work = unit.kernel_instances[k] * max(1, num_sets)
+    sm = summary
+    flops = sm["add"] + sm["sub"] + sm["mul"] + sm["neg"] + 2 * sm["fma"]
+    base = np.array([lg(work), lg(sm["entries"]), lg(sm["loads"]), float(sm["registers"]) / 64.0, lg(sm["bundles"]),
+                     sm["entries"] / max(1, sm["bundles"]), lg(flops), lg(sm["div"] + sm["rec"]), lg(sm["sqrt"]),
+                     lg(sm["st"]), float(unit.kernel_levels[k])], np.float32)
+    shp = np.array([math.log2(items), math.log2(lanes), math.log2(tpb) - 6.0], np.float32)
+    regfile = math.log2(1.0 + sm["registers"] * items / lanes)
+    return np.concatenate([base, shp, base[:5] * shp[0], base[:5] * shp[1], base[:5] * shp[2], [regfile]]).astype(np.float32)
+
+
+@dataclass
+class KernelTuneResult:
+    shapes: list                 # chosen shape per kernel
+    us: np.ndarray               # time of each kernel in its chosen shape
+    table: dict = field(default_factory=dict)  # shape -> per-kernel times (timed shapes only)
+    seconds: float = 0.0
+    timed: int = 0               # time_kernels passes
+
+    @property
+    def total_us(self) -> float:
+        return float(self.us.sum())
+
+
+def _apply_shapes(unit: native.Unit, shapes) -> None:
+    for k, (i, l, t) in enumerate(shapes):
+        unit.set_kernel_shape(k, i, l, t)
+
+
+def tune_kernels(unit: native.Unit, flush=None, shapes=None, reps: int = 5) -> KernelTuneResult:
+    """Exhaustive per-kernel tuning: every kernel timed in every shape."""
+    shapes = KERNEL_SHAPES if shapes is None else shapes
+    t0 = time.perf_counter()
+    nk = unit.num_kernels
+    table = {}
+    for sh in shapes:
+        _apply_shapes(unit, [sh] * nk)
+        try:
+            unit.time_kernels(1, flush)
+            table[sh] = unit.time_kernels(reps, flush)
+        except RuntimeError:
+            continue  # shape does not fit
+    best = [min(table, key=lambda sh: table[sh][k]) for k in range(nk)]
+    us = np.array([table[best[k]][k] for k in range(nk)])
+    _apply_shapes(unit, best)
+    return KernelTuneResult(best, us, table, time.perf_counter() - t0, len(table))
+
+
+class KernelCostModel(CostModel):
+    """MLP regression of log(kernel launch time in us) on kernel_features."""
+
+
+def propose_kernel_shapes(model: KernelCostModel, unit: native.Unit, num_sets: int, k_top: int, summaries) -> list:
+    """Top-k shapes per kernel by predicted time."""
+    out = []
+    for k in range(unit.num_kernels):
+        X = np.stack([kernel_features(unit, k, num_sets, sh, summaries[k]) for sh in KERNEL_SHAPES])
+        order = np.argsort(model.predict_us(X))
+        out.append([KERNEL_SHAPES[i] for i in order[:k_top]])
+    return out
+
+
+def tune_kernels_with_model(unit: native.Unit, model: KernelCostModel, num_sets: int, flush=None, k_top: int = 2,
+                            reps: int = 5) -> KernelTuneResult:
+    """Times only each kernel's top-k proposed shapes (k passes of
+    time_kernels, pass r putting every kernel in its r-th proposal)."""
+    t0 = time.perf_counter()
+    summaries = [program_summary(unit, k) for k in range(unit.num_kernels)]
+    props = propose_kernel_shapes(model, unit, num_sets, k_top, summaries)
+    nk = unit.num_kernels
+    best = [None] * nk
+    us = np.full(nk, np.inf)
+    passes = 0
+    for r in range(k_top):
+        _apply_shapes(unit, [p[r] for p in props])
+        try:
+            unit.time_kernels(1, flush)
+            t = unit.time_kernels(reps, flush)
+        except RuntimeError:
+            continue
+        passes += 1
+        for k in range(nk):
+            if t[k] < us[k]:
+                us[k], best[k] = t[k], props[k][r]
+    best = [b if b is not None else (1, 1, 128) for b in best]
+    _apply_shapes(unit, best)
+    return KernelTuneResult(best, us, {}, time.perf_counter() - t0, passes)

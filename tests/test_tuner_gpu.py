@@ -154,3 +154,62 @@ def test_learned_proposer_beats_untrained_choice():
     assert len(tuner.SPACE) / K >= 10
     assert np.mean(regret_model) <= 0.10
     assert np.mean(regret_model) < np.mean(regret_random)
+
+
+def test_per_kernel_shapes_are_exact_and_timed():
+    """Per-kernel launch shapes (plain and levels schedules) change no value;
+    per-kernel timing returns one positive time per launched kernel."""
+    torch = pytest.importorskip("torch")
+    for name, size, seed in [("cotan", 8, 22), ("cloth", 5, 32), ("neohookean", 2, 42)]:
+        _, inp, gold = load_golden(name, size)
+        w = native.Workload(name, size, seed)
+        u = native.Unit.from_workload(w)
+        for i, a in enumerate(split_inputs(w, inp)):
+            u.set_arg(i, a)
+        rng = np.random.default_rng(seed)
+        for trial in range(3):
+            for k in range(u.num_kernels):
+                i, l, t = tuner.KERNEL_SHAPES[rng.integers(len(tuner.KERNEL_SHAPES))]
+                u.set_kernel_shape(k, i, l, t)
+            for kind in (native.SCHEDULE_PLAIN, native.SCHEDULE_LEVELS):
+                u.set_schedule(kind=kind, math=native.MATH_EXACT)
+                u.run()
+                assert bits_equal(u.get_result(0), gold), (name, trial, kind)
+        flush = torch.empty(1 << 20, dtype=torch.float32, device="cuda")
+        t = u.time_kernels(3, flush)
+        assert len(t) == u.num_kernels
+        assert all(t[k] > 0 for k in range(u.num_kernels) if u.kernel_instances[k])
+        u.run()
+        assert bits_equal(u.get_result(0), gold)
+
+
+def test_per_kernel_tuning_picks_the_fastest_shape():
+    """tune_kernels keeps, per kernel, the shape of least time, and the learned
+    per-kernel proposer (trained on other units) lands within 10% of it."""
+    X, y = [], []
+    for spec in [("cloth", 10, 3), ("cotan", 60, 4), ("random", 40000, 5)]:
+        w = native.Workload(*spec)
+        u = native.Unit.from_workload(w)
+        for i, a in enumerate(w.inputs):
+            u.set_arg(i, a)
+        res = tuner.tune_kernels(u, reps=3)
+        sums = [tuner.program_summary(u, k) for k in range(u.num_kernels)]
+        for sh, t in res.table.items():
+            for k in range(u.num_kernels):
+                if u.kernel_instances[k] and t[k] > 0:
+                    X.append(tuner.kernel_features(u, k, 1, sh, sums[k]))
+                    y.append(t[k])
+    model = tuner.KernelCostModel(seed=1)
+    model.fit(np.stack(X), np.array(y), epochs=2000)
+    w = native.Workload("cloth", 14, 9)
+    u = native.Unit.from_workload(w)
+    for i, a in enumerate(w.inputs):
+        u.set_arg(i, a)
+    full = tuner.tune_kernels(u, reps=3)
+    for k in range(u.num_kernels):
+        if u.kernel_instances[k]:
+            assert full.us[k] == min(full.table[sh][k] for sh in full.table)
+    learned = tuner.tune_kernels_with_model(u, model, 1, k_top=2, reps=3)
+    total = sum(full.table[sh][k] for k, sh in enumerate(learned.shapes))
+    print("per-kernel regret", total / full.total_us - 1.0)
+    assert total <= 1.10 * full.total_us
