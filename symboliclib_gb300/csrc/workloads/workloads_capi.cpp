@@ -26,6 +26,8 @@ struct Workload {
     std::string planText;
     double frontSeconds = 0.0;
     std::uint64_t outputs = 0;
+    int rows = 0, cols = 0;              // output matrix (CSC workloads)
+    std::vector<int> colPtr, rowIdx;
 };
 
 thread_local std::string g_err;
@@ -77,6 +79,7 @@ int symgbw_build(const char* name, int size, unsigned long long seed, int vector
             w->inputs.push_back(A.values);
             w->numeric = ataPlusA(A, A.values).values;
             w->outputs = B.nnz();
+            w->rows = B.rows, w->cols = B.cols, w->colPtr = B.colPtr, w->rowIdx = B.rowIdx;
         } else if (n == "cotan") {
             TriMesh m = cotanMesh(size, seed);
             auto VS = variables(m.V.size(), 0);
@@ -86,6 +89,7 @@ int symgbw_build(const char* name, int size, unsigned long long seed, int vector
             w->inputs.push_back(m.V);
             w->numeric = cotanLaplacian(m.V, m.nv, m.F).values;
             w->outputs = L.nnz();
+            w->rows = L.rows, w->cols = L.cols, w->colPtr = L.colPtr, w->rowIdx = L.rowIdx;
         } else if (n == "cloth") {
             ClothRest r = clothRest(size);
             std::vector<double> X, vel;
@@ -99,6 +103,7 @@ int symgbw_build(const char* name, int size, unsigned long long seed, int vector
             w->inputs.push_back(vel);
             w->numeric = clothMatrix(r, X, vel, NoFix()).values;
             w->outputs = A.nnz();
+            w->rows = A.rows, w->cols = A.cols, w->colPtr = A.colPtr, w->rowIdx = A.rowIdx;
         } else if (n == "random") {
             Rng rng(seed ^ 0x5eedULL);
             const int m = std::max(8, size / 2);
@@ -123,6 +128,7 @@ int symgbw_build(const char* name, int size, unsigned long long seed, int vector
             w->inputs.push_back(X);
             w->numeric = symmetricFromUpper((int)X.size(), neoHookeanHessianUpper(m, X)).values;
             w->outputs = H.nnz();
+            w->rows = H.rows, w->cols = H.cols, w->colPtr = H.colPtr, w->rowIdx = H.rowIdx;
         } else {
             g_err = "unknown workload " + n;
             return -1;
@@ -167,5 +173,16 @@ uint64_t symgbw_plan_text(symgbw_t w, char* buf, uint64_t cap) {
     return w->planText.size();
 }
 double symgbw_front_seconds(symgbw_t w) { return w->frontSeconds; }
+
+// Pattern of the output matrix (CSC; 0 rows when the workload has none):
+// col_ptr has cols + 1 entries, row_idx nnz.
+int symgbw_pattern(symgbw_t w, int* rows, int* cols, const int** col_ptr, const int** row_idx) {
+    if (!w) return -1;
+    *rows = w->rows;
+    *cols = w->cols;
+    *col_ptr = w->colPtr.data();
+    *row_idx = w->rowIdx.data();
+    return 0;
+}
 
 }  // extern "C"

@@ -75,6 +75,11 @@ SYMGB_FUNCTIONS = {
                                    C.c_void_p]),
     "symgb_measure_fp64_rate": (C.c_int, [C.POINTER(C.c_double)]),
     "symgb_set_kernel_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "symgb_cg_create": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "symgb_cg_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_void_p,
+                                 C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "symgb_cg_multiply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "symgb_cg_destroy": (None, [C.c_void_p]),
     "symgb_time_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_double)]),
     "symgb_plan_save": (C.c_int, [C.c_char_p, C.POINTER(PlanDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
     "symgb_plan_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
@@ -149,6 +154,8 @@ def workloads() -> C.CDLL:
         lib.symgbw_plan_text.argtypes = [C.c_void_p, C.c_char_p, C.c_uint64]
         lib.symgbw_front_seconds.restype = C.c_double
         lib.symgbw_front_seconds.argtypes = [C.c_void_p]
+        lib.symgbw_pattern.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       C.POINTER(C.POINTER(C.c_int)), C.POINTER(C.POINTER(C.c_int))]
         lib._typed = True
     return lib
 
@@ -190,6 +197,15 @@ class Workload:
         p = lib.symgbw_numeric(h, C.byref(n))
         self.numeric = _array(p, n.value, np.float64)
         self.front_seconds = lib.symgbw_front_seconds(h)
+
+    def pattern(self):
+        """(rows, cols, col_ptr, row_idx) of the output matrix in CSC form."""
+        rows, cols = C.c_int(), C.c_int()
+        cp, ri = C.POINTER(C.c_int)(), C.POINTER(C.c_int)()
+        self._lib.symgbw_pattern(self.handle, C.byref(rows), C.byref(cols), C.byref(cp), C.byref(ri))
+        col_ptr = _array(cp, cols.value + 1, np.int32).astype(np.int64) if cols.value else np.zeros(1, np.int64)
+        row_idx = _array(ri, int(col_ptr[-1]), np.int32)
+        return rows.value, cols.value, col_ptr, row_idx
 
     @property
     def plan_text(self) -> str:
@@ -243,6 +259,38 @@ class PlanFile:
     def __del__(self):
         if getattr(self, "handle", None):
             self._lib.symgb_plan_file_free(self.handle)
+            self.handle = None
+
+
+class CG:
+    """Batched Jacobi-preconditioned conjugate gradient (symgb_cg_*) for S
+    symmetric positive definite systems sharing one CSC pattern; solve and
+    multiply take torch CUDA tensors (values [S, nnz], vectors [S, n])."""
+
+    def __init__(self, n: int, col_ptr, row_idx, lower_only: bool = True, num_sets: int = 1):
+        lib = symgb()
+        self._cp = np.ascontiguousarray(col_ptr, np.int64)
+        self._ri = np.ascontiguousarray(row_idx, np.int32)
+        h = C.c_void_p()
+        check(lib.symgb_cg_create(n, self._cp.ctypes.data, self._ri.ctypes.data, int(lower_only), num_sets,
+                                  C.byref(h)))
+        self._lib, self.handle, self.n, self.num_sets = lib, h, n, num_sets
+
+    def solve(self, values, b, x, tol: float = 1e-10, max_iter: int = 1000, stream=None):
+        it, res = C.c_int(), C.c_double()
+        st = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        check(self._lib.symgb_cg_solve(self.handle, C.c_void_p(values.data_ptr()), C.c_void_p(b.data_ptr()),
+                                       C.c_void_p(x.data_ptr()), tol, max_iter, st, C.byref(it), C.byref(res)))
+        return it.value, res.value
+
+    def multiply(self, values, p, q, stream=None) -> None:
+        st = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        check(self._lib.symgb_cg_multiply(self.handle, C.c_void_p(values.data_ptr()), C.c_void_p(p.data_ptr()),
+                                          C.c_void_p(q.data_ptr()), st))
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            self._lib.symgb_cg_destroy(self.handle)
             self.handle = None
 
 

@@ -15,6 +15,9 @@
         per-kernel launch shapes: the kernel-level MLP (trained on other
         units' per-kernel timings) against exhaustive per-kernel tuning, and
         the tuned runs against the best unit-wide schedule.
+    python -m symboliclib_gb300.report solve --size 300 --sets 8
+        the cloth system matrix assembled by the engine, then solved on the
+        device by the batched conjugate gradient; SciPy's CG as CPU reference.
 Each prints one JSON line.  Errors are measured against the workload's FP64
 model evaluated in double (floor 1e-4 of the largest magnitude).
 """
@@ -290,6 +293,60 @@ def kernels(args):
         "max_rel_err": err}), flush=True)
 
 
+def solve(args):
+    """Assembly of the cloth system matrix by the engine, then the batched
+    conjugate-gradient solve on the device; SciPy's CG on the host for one
+    system as the CPU reference."""
+    import torch
+    from scipy.sparse import csc_matrix
+    from scipy.sparse.linalg import cg as scipy_cg
+    w = native.Workload("cloth", args.size, args.seed)
+    S = args.sets
+    u = native.Unit.from_workload(w)
+    u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_FAST, items_per_thread=1, lanes_per_item=2,
+                   threads_per_block=64)
+    u.set_num_sets(S)
+    for i, a in enumerate(w.inputs):
+        u.set_arg(i, np.tile(a, S))
+    u.run()
+    nnz = len(w.numeric)
+    vals = torch.empty((S, nnz), dtype=torch.float64, device="cuda")
+    native.check(native.symgb().symgb_get_result_sets_device(u.handle, C.c_void_p(vals.data_ptr()), 0))
+    r, c, cp, ri = w.pattern()
+    rng = np.random.default_rng(args.seed)
+    b = torch.from_numpy(rng.standard_normal((S, r))).cuda()
+    x = torch.empty_like(b)
+    cg = native.CG(r, cp, ri, True, S)
+    cg.solve(vals, b, x, args.tol, 20)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    it, res = cg.solve(vals, b, x, args.tol, args.max_iter)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    nnz_full = 2 * nnz - r
+    per_iter_bytes = S * (8 * nnz_full + 104 * r) + 4 * nnz_full + 8 * (r + 1)
+    # CPU reference: SciPy CG (one system, no preconditioner argument needed to compare work per iteration)
+    L = csc_matrix((w.numeric, ri, cp), shape=(r, c))
+    A = (L + L.T - csc_matrix((L.diagonal(), (np.arange(r), np.arange(r))), shape=(r, r))).tocsr()
+    bh = b[0].cpu().numpy()
+    t1 = time.perf_counter()
+    it_cpu = [0]
+    count = lambda _: it_cpu.__setitem__(0, it_cpu[0] + 1)
+    try:
+        xs, info = scipy_cg(A, bh, rtol=args.tol, maxiter=args.max_iter, callback=count)
+    except TypeError:  # SciPy before 1.12 names the tolerance `tol`
+        xs, info = scipy_cg(A, bh, tol=args.tol, maxiter=args.max_iter, callback=count)
+    t_cpu = time.perf_counter() - t1
+    resid = float(np.linalg.norm(A @ x[0].cpu().numpy() - bh) / np.linalg.norm(bh))
+    print(json.dumps({
+        "workload": f"cloth {args.size}", "unknowns": r, "nnz_lower": nnz, "nnz_full": nnz_full, "systems": S,
+        "gpu": {"iterations": it, "max_rel_residual": res, "seconds": t, "us_per_iteration": t / max(1, it) * 1e6,
+                "bytes_per_iteration": per_iter_bytes, "hbm_gbs": per_iter_bytes * it / t / 1e9,
+                "hbm_frac": per_iter_bytes * it / t / 1e9 / hbm_peak(), "checked_residual_set0": resid},
+        "cpu_scipy_cg_one_system": {"iterations": it_cpu[0], "seconds": t_cpu, "info": int(info)},
+        "speedup_per_system": (t_cpu / max(1, it_cpu[0])) / (t / max(1, it) / S)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -325,8 +382,14 @@ def main():
     d.add_argument("--k", type=int, default=2)
     d.add_argument("--epochs", type=int, default=4000)
     d.add_argument("--seed", type=int, default=5)
+    e = sub.add_parser("solve")
+    e.add_argument("--size", type=int, default=300)
+    e.add_argument("--sets", type=int, default=8)
+    e.add_argument("--tol", type=float, default=1e-10)
+    e.add_argument("--max-iter", type=int, default=5000)
+    e.add_argument("--seed", type=int, default=3)
     args = ap.parse_args()
-    {"single": single, "batch": batch, "learned": learned, "kernels": kernels}[args.cmd](args)
+    {"single": single, "batch": batch, "learned": learned, "kernels": kernels, "solve": solve}[args.cmd](args)
 
 
 if __name__ == "__main__":
