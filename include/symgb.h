@@ -254,25 +254,29 @@ const double* symgb_plan_file_const_data(symgb_plan_file_t f);
 void symgb_plan_file_free(symgb_plan_file_t f);
 const char* symgb_plan_last_error(void);
 
-/* The step after assembly: batched Jacobi-preconditioned conjugate gradient
- * for symmetric positive definite A x = b (the reference's cloth example
- * assembles A = M - h (D + h K) and b for an implicit step,
+/* The step after assembly: batched Jacobi-preconditioned Krylov solves of
+ * A x = b for symmetric A (the reference's cloth example assembles
+ * A = M - h (D + h K) and b for an implicit step,
  * examples/BaraffWitkin/implementation/cloth.cpp:96-111, and keeps the lower
  * triangle of A, examples/BaraffWitkin/main.cpp:56).  The pattern is given
  * once on the host as CSC (col_ptr[n + 1], row_idx[nnz]; lower_only = 1 for a
  * lower triangle, 0 for the full matrix); num_sets systems (1..256) share it.
- * symgb_cg_solve takes device pointers: values [set][nnz] in the pattern's
- * order (e.g. symgb_get_result_sets_device of the unit that assembles A),
- * b and x [set][n]; it stops once every system's |r| / |b| <= tol (checked
- * every 16 iterations) or after max_iter iterations, starting from x = 0.
- * symgb_cg_multiply computes q = A p for the same layouts. */
-typedef struct symgb_cg* symgb_cg_t;
-int symgb_cg_create(int64_t n, const int64_t* col_ptr, const int32_t* row_idx, int lower_only, int num_sets,
-                    symgb_cg_t* out);
-int symgb_cg_solve(symgb_cg_t s, const double* values, const double* b, double* x, double tol, int max_iter,
-                   void* stream, int* iterations, double* max_rel_residual);
-int symgb_cg_multiply(symgb_cg_t s, const double* values, const double* p, double* q, void* stream);
-void symgb_cg_destroy(symgb_cg_t s);
+ * symgb_solver_solve takes device pointers: values [set][nnz] in the
+ * pattern's order (e.g. symgb_get_result_sets_device of the unit that
+ * assembles A), b and x [set][n].  Methods: conjugate gradient (A positive
+ * definite) or BiCGSTAB (any nonsingular A; the cloth matrices of a deformed
+ * sheet are indefinite).  It starts from x = 0 and stops once every system's
+ * |r| / |b| <= tol (checked every 16 iterations) or after max_iter
+ * iterations, reporting both.  symgb_solver_multiply computes q = A p. */
+#define SYMGB_SOLVER_CG 0
+#define SYMGB_SOLVER_BICGSTAB 1
+typedef struct symgb_solver* symgb_solver_t;
+int symgb_solver_create(int64_t n, const int64_t* col_ptr, const int32_t* row_idx, int lower_only, int num_sets,
+                        symgb_solver_t* out);
+int symgb_solver_solve(symgb_solver_t s, int method, const double* values, const double* b, double* x, double tol,
+                       int max_iter, void* stream, int* iterations, double* max_rel_residual);
+int symgb_solver_multiply(symgb_solver_t s, const double* values, const double* p, double* q, void* stream);
+void symgb_solver_destroy(symgb_solver_t s);
 
 /* Measured FP64 FMA throughput of the current device (FLOP/s, one FMA = 2). */
 int symgb_measure_fp64_rate(double* flops_per_second);

@@ -75,11 +75,11 @@ SYMGB_FUNCTIONS = {
                                    C.c_void_p]),
     "symgb_measure_fp64_rate": (C.c_int, [C.POINTER(C.c_double)]),
     "symgb_set_kernel_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
-    "symgb_cg_create": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
-    "symgb_cg_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_void_p,
-                                 C.POINTER(C.c_int), C.POINTER(C.c_double)]),
-    "symgb_cg_multiply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
-    "symgb_cg_destroy": (None, [C.c_void_p]),
+    "symgb_solver_create": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "symgb_solver_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
+                                     C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "symgb_solver_multiply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "symgb_solver_destroy": (None, [C.c_void_p]),
     "symgb_time_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_double)]),
     "symgb_plan_save": (C.c_int, [C.c_char_p, C.POINTER(PlanDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
     "symgb_plan_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
@@ -262,35 +262,40 @@ class PlanFile:
             self.handle = None
 
 
-class CG:
-    """Batched Jacobi-preconditioned conjugate gradient (symgb_cg_*) for S
-    symmetric positive definite systems sharing one CSC pattern; solve and
-    multiply take torch CUDA tensors (values [S, nnz], vectors [S, n])."""
+SOLVER_CG, SOLVER_BICGSTAB = 0, 1
+
+
+class SparseSolver:
+    """Batched Jacobi-preconditioned Krylov solves (symgb_solver_*) for S
+    symmetric systems sharing one CSC pattern: conjugate gradient (positive
+    definite) or BiCGSTAB (indefinite); solve and multiply take torch CUDA
+    tensors (values [S, nnz], vectors [S, n])."""
 
     def __init__(self, n: int, col_ptr, row_idx, lower_only: bool = True, num_sets: int = 1):
         lib = symgb()
         self._cp = np.ascontiguousarray(col_ptr, np.int64)
         self._ri = np.ascontiguousarray(row_idx, np.int32)
         h = C.c_void_p()
-        check(lib.symgb_cg_create(n, self._cp.ctypes.data, self._ri.ctypes.data, int(lower_only), num_sets,
-                                  C.byref(h)))
+        check(lib.symgb_solver_create(n, self._cp.ctypes.data, self._ri.ctypes.data, int(lower_only), num_sets,
+                                      C.byref(h)))
         self._lib, self.handle, self.n, self.num_sets = lib, h, n, num_sets
 
-    def solve(self, values, b, x, tol: float = 1e-10, max_iter: int = 1000, stream=None):
+    def solve(self, values, b, x, tol: float = 1e-10, max_iter: int = 1000, method: int = SOLVER_CG, stream=None):
+        """Returns (iterations, largest relative residual over the systems)."""
         it, res = C.c_int(), C.c_double()
         st = C.c_void_p(stream.cuda_stream) if stream is not None else None
-        check(self._lib.symgb_cg_solve(self.handle, C.c_void_p(values.data_ptr()), C.c_void_p(b.data_ptr()),
-                                       C.c_void_p(x.data_ptr()), tol, max_iter, st, C.byref(it), C.byref(res)))
+        check(self._lib.symgb_solver_solve(self.handle, method, C.c_void_p(values.data_ptr()), C.c_void_p(b.data_ptr()),
+                                           C.c_void_p(x.data_ptr()), tol, max_iter, st, C.byref(it), C.byref(res)))
         return it.value, res.value
 
     def multiply(self, values, p, q, stream=None) -> None:
         st = C.c_void_p(stream.cuda_stream) if stream is not None else None
-        check(self._lib.symgb_cg_multiply(self.handle, C.c_void_p(values.data_ptr()), C.c_void_p(p.data_ptr()),
-                                          C.c_void_p(q.data_ptr()), st))
+        check(self._lib.symgb_solver_multiply(self.handle, C.c_void_p(values.data_ptr()), C.c_void_p(p.data_ptr()),
+                                              C.c_void_p(q.data_ptr()), st))
 
     def __del__(self):
         if getattr(self, "handle", None):
-            self._lib.symgb_cg_destroy(self.handle)
+            self._lib.symgb_solver_destroy(self.handle)
             self.handle = None
 
 

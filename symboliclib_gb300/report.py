@@ -17,7 +17,8 @@
         the tuned runs against the best unit-wide schedule.
     python -m symboliclib_gb300.report solve --size 300 --sets 8
         the cloth system matrix assembled by the engine, then solved on the
-        device by the batched conjugate gradient; SciPy's CG as CPU reference.
+        device by the batched BiCGSTAB (the matrix is indefinite) or CG; SciPy's
+        solver of the same method as CPU reference.
 Each prints one JSON line.  Errors are measured against the workload's FP64
 model evaluated in double (floor 1e-4 of the largest magnitude).
 """
@@ -316,16 +317,21 @@ def solve(args):
     rng = np.random.default_rng(args.seed)
     b = torch.from_numpy(rng.standard_normal((S, r))).cuda()
     x = torch.empty_like(b)
-    cg = native.CG(r, cp, ri, True, S)
-    cg.solve(vals, b, x, args.tol, 20)  # warm-up
+    solver = native.SparseSolver(r, cp, ri, True, S)
+    method = native.SOLVER_BICGSTAB if args.method == "bicgstab" else native.SOLVER_CG
+    solver.solve(vals, b, x, args.tol, 20, method)  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    it, res = cg.solve(vals, b, x, args.tol, args.max_iter)
+    it, res = solver.solve(vals, b, x, args.tol, args.max_iter, method)
     torch.cuda.synchronize()
     t = time.perf_counter() - t0
     nnz_full = 2 * nnz - r
-    per_iter_bytes = S * (8 * nnz_full + 104 * r) + 4 * nnz_full + 8 * (r + 1)
-    # CPU reference: SciPy CG (one system, no preconditioner argument needed to compare work per iteration)
+    # per iteration: BiCGSTAB two matrix products and ~26 vector passes, CG one and ~13
+    mats, vecs = (2, 26) if method == native.SOLVER_BICGSTAB else (1, 13)
+    per_iter_bytes = mats * (S * 8 * nnz_full + 4 * nnz_full + 8 * (r + 1)) + S * vecs * 8 * r
+    # CPU reference: SciPy's solver of the same method, one system
+    from scipy.sparse.linalg import bicgstab as scipy_bicgstab
+    cpu_solver = scipy_bicgstab if method == native.SOLVER_BICGSTAB else scipy_cg
     L = csc_matrix((w.numeric, ri, cp), shape=(r, c))
     A = (L + L.T - csc_matrix((L.diagonal(), (np.arange(r), np.arange(r))), shape=(r, r))).tocsr()
     bh = b[0].cpu().numpy()
@@ -333,9 +339,9 @@ def solve(args):
     it_cpu = [0]
     count = lambda _: it_cpu.__setitem__(0, it_cpu[0] + 1)
     try:
-        xs, info = scipy_cg(A, bh, rtol=args.tol, maxiter=args.max_iter, callback=count)
+        xs, info = cpu_solver(A, bh, rtol=args.tol, maxiter=args.max_iter, callback=count)
     except TypeError:  # SciPy before 1.12 names the tolerance `tol`
-        xs, info = scipy_cg(A, bh, tol=args.tol, maxiter=args.max_iter, callback=count)
+        xs, info = cpu_solver(A, bh, tol=args.tol, maxiter=args.max_iter, callback=count)
     t_cpu = time.perf_counter() - t1
     resid = float(np.linalg.norm(A @ x[0].cpu().numpy() - bh) / np.linalg.norm(bh))
     print(json.dumps({
@@ -343,7 +349,8 @@ def solve(args):
         "gpu": {"iterations": it, "max_rel_residual": res, "seconds": t, "us_per_iteration": t / max(1, it) * 1e6,
                 "bytes_per_iteration": per_iter_bytes, "hbm_gbs": per_iter_bytes * it / t / 1e9,
                 "hbm_frac": per_iter_bytes * it / t / 1e9 / hbm_peak(), "checked_residual_set0": resid},
-        "cpu_scipy_cg_one_system": {"iterations": it_cpu[0], "seconds": t_cpu, "info": int(info)},
+        "method": args.method,
+        "cpu_scipy_one_system": {"iterations": it_cpu[0], "seconds": t_cpu, "info": int(info)},
         "speedup_per_system": (t_cpu / max(1, it_cpu[0])) / (t / max(1, it) / S)}), flush=True)
 
 
@@ -388,6 +395,7 @@ def main():
     e.add_argument("--tol", type=float, default=1e-10)
     e.add_argument("--max-iter", type=int, default=5000)
     e.add_argument("--seed", type=int, default=3)
+    e.add_argument("--method", default="bicgstab", choices=["cg", "bicgstab"])
     args = ap.parse_args()
     {"single": single, "batch": batch, "learned": learned, "kernels": kernels, "solve": solve}[args.cmd](args)
 

@@ -1,0 +1,126 @@
+"""The solve after assembly: batched Krylov solves on the cloth system matrix
+(lower triangle, as the engine's cloth workload outputs it), checked against
+dense NumPy linear algebra.  The cloth matrices of the deformed synthetic
+sheet are symmetric indefinite, so conjugate gradient is exercised on a
+positive definite shift of them and BiCGSTAB on the matrices themselves."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from symboliclib_gb300 import native
+
+
+def dense(w, values):
+    r, c, cp, ri = w.pattern()
+    L = np.zeros((r, c))
+    for j in range(c):
+        for e in range(cp[j], cp[j + 1]):
+            L[ri[e], j] = values[e]
+    return L + L.T - np.diag(np.diag(L))
+
+
+def shifted(w, shift):
+    """Lower-triangle values of A + shift I (positive definite for a shift
+    above -(smallest eigenvalue))."""
+    r, c, cp, ri = w.pattern()
+    v = w.numeric.copy()
+    for j in range(c):
+        for e in range(cp[j], cp[j + 1]):
+            if ri[e] == j:
+                v[e] += shift
+    return v
+
+
+def test_bad_patterns_are_rejected():
+    lib = native.symgb()
+    h = C.c_void_p()
+    cp = np.array([0, 2, 3], np.int64)
+    ri = np.array([0, 1, 0], np.int32)  # column 1 holds row 0: above the diagonal
+    assert lib.symgb_solver_create(2, cp.ctypes.data, ri.ctypes.data, 1, 1, C.byref(h)) == -1  # SYMGB_ERR_ARGUMENT
+    bad = np.array([0, 1, 5], np.int32)  # row index out of range
+    assert lib.symgb_solver_create(2, cp.ctypes.data, bad.ctypes.data, 0, 1, C.byref(h)) == -1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("sets", [1, 3])
+def test_multiply_matches_dense(sets):
+    torch = pytest.importorskip("torch")
+    w = native.Workload("cloth", 8, 5)
+    r, c, cp, ri = w.pattern()
+    vals = np.stack([w.numeric * (1.0 + 0.1 * s) for s in range(sets)])
+    p = np.random.default_rng(1).standard_normal((sets, r))
+    solver = native.SparseSolver(r, cp, ri, True, sets)
+    q = torch.empty((sets, r), dtype=torch.float64, device="cuda")
+    solver.multiply(torch.from_numpy(vals).cuda(), torch.from_numpy(p).cuda(), q)
+    for s in range(sets):
+        A = dense(w, vals[s])
+        assert np.max(np.abs(q[s].cpu().numpy() - A @ p[s]) / (np.abs(A) @ np.abs(p[s]))) <= 1e-14
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", [native.SOLVER_CG, native.SOLVER_BICGSTAB])
+@pytest.mark.parametrize("size,sets", [(5, 1), (12, 4)])
+def test_solve_matches_dense(size, sets, method):
+    torch = pytest.importorskip("torch")
+    w = native.Workload("cloth", size, 11)
+    r, c, cp, ri = w.pattern()
+    base = shifted(w, 0.5) if method == native.SOLVER_CG else w.numeric
+    vals = np.stack([base * (1.0 + 0.05 * s) for s in range(sets)])
+    if method == native.SOLVER_CG:
+        assert np.linalg.eigvalsh(dense(w, vals[0])).min() > 0
+    b = np.random.default_rng(2).standard_normal((sets, r))
+    solver = native.SparseSolver(r, cp, ri, True, sets)
+    x = torch.empty((sets, r), dtype=torch.float64, device="cuda")
+    it, res = solver.solve(torch.from_numpy(vals).cuda(), torch.from_numpy(b).cuda(), x, tol=1e-12, max_iter=20000,
+                           method=method)
+    assert res <= 1e-12 and 0 < it <= 20000
+    # The recurrence residual of BiCGSTAB drifts from b - A x over thousands of
+    # iterations (condition number ~1e5 here); the true residual is checked
+    # to 1e-9, and the solution against the dense one to the condition number
+    # times that.
+    true_tol = 1e-11 if method == native.SOLVER_CG else 1e-9
+    for s in range(sets):
+        A = dense(w, vals[s])
+        xs = x[s].cpu().numpy()
+        assert np.linalg.norm(A @ xs - b[s]) <= true_tol * np.linalg.norm(b[s])
+        ref = np.linalg.solve(A, b[s])
+        assert np.linalg.norm(xs - ref) <= true_tol * np.linalg.cond(A) * np.linalg.norm(ref)
+
+
+@pytest.mark.gpu
+def test_assembly_then_solve_on_the_device():
+    """A assembled by the engine (results left on the device) feeds the solver."""
+    torch = pytest.importorskip("torch")
+    w = native.Workload("cloth", 10, 3)
+    sets = 2
+    u = native.Unit.from_workload(w)
+    u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_FAST)
+    u.set_num_sets(sets)
+    for i, a in enumerate(w.inputs):
+        u.set_arg(i, np.tile(a, sets))
+    u.run()
+    nnz = len(w.numeric)
+    vals = torch.empty((sets, nnz), dtype=torch.float64, device="cuda")
+    native.check(native.symgb().symgb_get_result_sets_device(u.handle, C.c_void_p(vals.data_ptr()), 0))
+    r, c, cp, ri = w.pattern()
+    b = torch.ones((sets, r), dtype=torch.float64, device="cuda")
+    x = torch.empty_like(b)
+    solver = native.SparseSolver(r, cp, ri, True, sets)
+    it, res = solver.solve(vals, b, x, tol=1e-11, max_iter=20000, method=native.SOLVER_BICGSTAB)
+    assert res <= 1e-11
+    A = dense(w, w.numeric)
+    assert np.linalg.norm(A @ x[1].cpu().numpy() - 1.0) <= 1e-8 * np.sqrt(r)
+
+
+@pytest.mark.gpu
+def test_iteration_limit_reports_the_residual():
+    torch = pytest.importorskip("torch")
+    w = native.Workload("cloth", 12, 11)
+    r, c, cp, ri = w.pattern()
+    solver = native.SparseSolver(r, cp, ri, True, 1)
+    x = torch.empty((1, r), dtype=torch.float64, device="cuda")
+    vals = torch.from_numpy(w.numeric[None, :].copy()).cuda()
+    it, res = solver.solve(vals, torch.ones((1, r), dtype=torch.float64, device="cuda"), x, 1e-14, 3,
+                           method=native.SOLVER_BICGSTAB)
+    assert it == 3 and res > 1e-14
