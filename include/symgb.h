@@ -180,6 +180,14 @@ int symgb_run_async(symgb_unit_t u);
 int symgb_set_arg_sets_device(symgb_unit_t u, const double* d, int i);
 int symgb_get_result_sets_device(symgb_unit_t u, double* d, int k);
 int symgb_synchronize(symgb_unit_t u);
+/* Asynchronous host transfers, for overlapping one execute's transfers with
+ * another's evaluation: `d` must be page-locked host memory (cudaHostAlloc or
+ * cudaHostRegister; anything else is SYMGB_ERR_ARGUMENT).  The input copy, or
+ * the result gather written straight into `d`, is enqueued on the unit's
+ * stream; `d` must not be touched before symgb_synchronize (or a later event
+ * on that stream). */
+int symgb_set_arg_sets_async(symgb_unit_t u, const double* d, int i);
+int symgb_get_result_sets_async(symgb_unit_t u, double* d, int k);
 
 /* Batches of units (many patterns of uneven size): one evaluation of every
  * unit, each with its own schedule and value sets, captured into one CUDA graph

@@ -568,6 +568,31 @@ int symgb_set_arg_sets(symgb_unit_t u, const double* d, int i) {
     return SYMGB_OK;
 }
 
+int symgb_set_arg_sets_async(symgb_unit_t u, const double* d, int i) {
+    if (!u || !u->initialized) return fail(SYMGB_ERR_STATE, "set_arg before init");
+    if (i < 0 || (std::size_t)i >= u->argStart.size() || !d) return fail(SYMGB_ERR_ARGUMENT, "bad argument index");
+    if (!mappedHost(const_cast<double*>(d))) return fail(SYMGB_ERR_ARGUMENT, "async set_arg needs page-locked memory");
+    const std::size_t n = u->argLength[i] * (std::size_t)u->numSets;
+    if (u->numSets == 1) {
+        SYMGB_CUDA(cudaMemcpyAsync(u->x.ptr + u->argStart[i], d, n * 8, cudaMemcpyHostToDevice, u->stream));
+        return SYMGB_OK;
+    }
+    if (u->staging.count < n) {
+        SYMGB_CUDA(cudaStreamSynchronize(u->stream));  // the staging buffer may be in use
+        SYMGB_CUDA(u->staging.alloc(n));
+    }
+    SYMGB_CUDA(cudaMemcpyAsync(u->staging.ptr, d, n * 8, cudaMemcpyHostToDevice, u->stream));
+    return symgb_set_arg_sets_device(u, u->staging.ptr, i);
+}
+
+int symgb_get_result_sets_async(symgb_unit_t u, double* d, int k) {
+    if (!u || !u->initialized) return fail(SYMGB_ERR_STATE, "get_result before init");
+    if (k < 0 || (std::size_t)k >= u->outStart.size() || !d) return fail(SYMGB_ERR_ARGUMENT, "bad result index");
+    double* dd = mappedHost(d);
+    if (!dd) return fail(SYMGB_ERR_ARGUMENT, "async get_result needs page-locked memory");
+    return symgb_get_result_sets_device(u, dd, k);
+}
+
 int symgb_finish(symgb_unit_t u) {
     if (!u) return fail(SYMGB_ERR_ARGUMENT, "null unit");
     if (u->initialized) cudaStreamSynchronize(u->stream);

@@ -75,6 +75,8 @@ SYMGB_FUNCTIONS = {
                                    C.c_void_p]),
     "symgb_measure_fp64_rate": (C.c_int, [C.POINTER(C.c_double)]),
     "symgb_set_kernel_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "symgb_set_arg_sets_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "symgb_get_result_sets_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "symgb_solver_create": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "symgb_solver_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
                                      C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]),

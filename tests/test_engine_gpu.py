@@ -164,6 +164,38 @@ def test_results_into_page_locked_memory(sets):
     assert bits_equal(pinned.numpy()[:len(gold)], gold)
 
 
+def test_async_transfers_between_two_units():
+    """Two units of one plan on two streams, fed and read with the async
+    page-locked calls in alternation (the pipelined end-to-end pattern):
+    every step's results equal the golden ones; pageable memory is refused."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    _, inp, gold = load_golden("cloth", 5)
+    w = native.Workload("cloth", 5, 32)
+    lib = native.symgb()
+    units = []
+    for _ in range(2):
+        u = native.Unit.from_workload(w)
+        u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_EXACT)
+        st = torch.cuda.Stream()
+        native.check(lib.symgb_set_stream(u.handle, C.c_void_p(st.cuda_stream)))
+        ins = [torch.from_numpy(a.copy()).pin_memory() for a in split_inputs(w, inp)]
+        outs = [torch.full((len(gold),), -1.0, dtype=torch.float64).pin_memory() for _ in range(3)]
+        units.append((u, st, ins, outs))
+    for k in range(6):
+        u, st, ins, outs = units[k % 2]
+        for i, a in enumerate(ins):
+            native.check(lib.symgb_set_arg_sets_async(u.handle, C.c_void_p(a.data_ptr()), i))
+        native.check(lib.symgb_run_async(u.handle))
+        native.check(lib.symgb_get_result_sets_async(u.handle, C.c_void_p(outs[k // 2].data_ptr()), 0))
+    for u, _, _, outs in units:
+        native.check(lib.symgb_synchronize(u.handle))
+        for o in outs:
+            assert bits_equal(o.numpy(), gold)
+    page = np.empty(len(gold))
+    assert lib.symgb_get_result_sets_async(units[0][0].handle, page.ctypes.data, 0) == -1
+
+
 def test_larger_cases_match_oracle():
     """Sizes beyond the fixtures: engine exact mode vs the CPU oracle."""
     for name, size, seed in [("cotan", 60, 5), ("ata", 30, 6), ("cloth", 12, 7)]:
