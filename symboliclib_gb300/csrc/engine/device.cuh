@@ -14,7 +14,7 @@ namespace symgb {
 namespace engine {
 
 struct DevKernel {
-    const std::uint64_t* prog;  // device program: loads section, then compute words
+    const std::uint64_t* prog;  // device program: load section, compute bundles, literal table
     const std::uint32_t* p;     // index table of this kernel
     const double* c;            // constant table of this kernel
     std::uint64_t yoff;         // first x slot written by this kernel

@@ -354,6 +354,9 @@ int checkDeviceError(symgb_unit* u) {
 
 int copyDesc(symgb_unit* u, const symgb_plan_desc* d) {
     if (!d || (d->num_kernels && !d->kernels)) return fail(SYMGB_ERR_ARGUMENT, "null plan");
+    // The interpreter addresses x slots with 32-bit indices (as the
+    // reference's u32 positionData does).
+    if (d->num_total_memory > 0xffffffffull) return fail(SYMGB_ERR_ARGUMENT, "plan needs more than 2^32 x slots");
     u->kernels.resize(d->num_kernels);
     int maxLevel = -1;
     for (std::uint32_t k = 0; k < d->num_kernels; ++k) {
