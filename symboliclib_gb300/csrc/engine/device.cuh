@@ -405,10 +405,13 @@ __device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t
 // Runs the tiles of segments [segBegin, segEnd); a grid barrier separates
 // segments (cooperative launches only when the range holds several segments).
 // Register cap per variant: the interpreter's occupancy is what hides the
-// latency of its shared-memory operands and FP64 results.
+// latency of its shared-memory operands and FP64 results.  With a cap of 72,
+// ptxas fits the two-item variant without library operations into 64
+// registers with no spills (96 allowed it 80; cotan 500 per execute: 153 us
+// against 163 us).
 template <int ITEMS>
 struct EvalRegs {
-    static constexpr int value = ITEMS == 1 ? 64 : ITEMS == 2 ? 96 : 128;
+    static constexpr int value = ITEMS == 1 ? 64 : ITEMS == 2 ? 72 : 96;
 };
 
 template <int ITEMS, int LANES, int MODE>
