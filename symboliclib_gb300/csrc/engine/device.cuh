@@ -248,6 +248,49 @@ __device__ bool gridBarrier(BarrierState* bar, int* hostError, unsigned long lon
 }
 
 
+// Load entries first, first + P, ..., first + (W - 1) P of the load section
+// (this lane's share of W rounds; entries past the end are skipped): all
+// index loads, then all gathers, then the register writes, so up to W x ITEMS
+// independent loads are in flight.  x slots fit in 32 bits (checked when the
+// unit is created).
+template <int W, int ITEMS, int MODE>
+__device__ __forceinline__ void runLoads(const std::uint64_t* prog, unsigned first, unsigned nl, unsigned P,
+                                         const DevKernel& k, const EvalArgs& A, const std::uint64_t (&ii)[ITEMS],
+                                         const unsigned (&ss)[ITEMS], const RegFile& rf) {
+    using namespace symgb::engine;
+    unsigned meta[W];
+    unsigned slot[W][ITEMS];
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+        const std::uint64_t w = (first + u * P < nl) ? prog[first + u * P] : 0ull;
+        meta[u] = (unsigned)w & 0xffffu;  // op, destination register
+        const unsigned op = (unsigned)w & 0xffu;
+        const unsigned imm = (unsigned)(w >> 32);
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j)
+            slot[u][j] = op == OP_LDX ? __ldg(k.p + ((unsigned)(w >> 16) & 0xffffu) * k.n + ii[j]) + imm : imm;
+    }
+    double v[W][ITEMS];
+#pragma unroll
+    for (int u = 0; u < W; ++u)
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            const unsigned op = meta[u] & 0xffu;
+            if (op == OP_LDX)
+                v[u][j] = loadX<MODE & MODE_L2>(A.x + (std::uint64_t)slot[u][j] * A.S + ss[j]);
+            else if (op == OP_LDC)
+                v[u][j] = __ldg(k.c + (std::uint64_t)slot[u][j] * k.n + ii[j]);
+            else
+                v[u][j] = 0.0;
+        }
+#pragma unroll
+    for (int u = 0; u < W; ++u)
+        if (first + u * P < nl) {
+#pragma unroll
+            for (int j = 0; j < ITEMS; ++j) rf.at(meta[u] >> 8, j) = v[u][j];
+        }
+}
+
 // Evaluates one tile.  A work item (one instance for one value set) is run by
 // P = LANES threads of one warp: warp lane l serves item slot l % (32 / P)
 // of its warp as lane l / (32 / P), so each half-warp touches consecutive
@@ -289,42 +332,21 @@ __device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t
                 ss[j] = (unsigned)(w - ii[j] * S);
             }
         }
-        // Loads: up to 8 entries at a time, all index loads, then all gathers.
-        // x slots fit in 32 bits (checked when the unit is created).
+        // Loads: in rounds of 8, 4, 2 and 1 entries per lane (the same count on
+        // every lane), all index loads, then all gathers.
         const unsigned nl = k.nloads;
-        for (unsigned b = lane; b < nl; b += 8 * P) {
-            unsigned meta[8];
-            unsigned slot[8][ITEMS];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const std::uint64_t w = (b + u * P < nl) ? prog[b + u * P] : 0ull;
-                meta[u] = (unsigned)w & 0xffffu;  // op, destination register
-                const unsigned op = (unsigned)w & 0xffu;
-                const unsigned imm = (unsigned)(w >> 32);
-#pragma unroll
-                for (int j = 0; j < ITEMS; ++j)
-                    slot[u][j] = op == OP_LDX ? __ldg(k.p + ((unsigned)(w >> 16) & 0xffffu) * k.n + ii[j]) + imm : imm;
-            }
-            double v[8][ITEMS];
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-#pragma unroll
-                for (int j = 0; j < ITEMS; ++j) {
-                    const unsigned op = meta[u] & 0xffu;
-                    if (op == OP_LDX)
-                        v[u][j] = loadX<MODE & MODE_L2>(A.x + (std::uint64_t)slot[u][j] * S + ss[j]);
-                    else if (op == OP_LDC)
-                        v[u][j] = __ldg(k.c + (std::uint64_t)slot[u][j] * k.n + ii[j]);
-                    else
-                        v[u][j] = 0.0;
-                }
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (b + u * P < nl) {
-#pragma unroll
-                    for (int j = 0; j < ITEMS; ++j) rf.at(meta[u] >> 8, j) = v[u][j];
-                }
+        const unsigned rounds = (nl + P - 1) / P;
+        unsigned r = 0;
+        for (; r + 8 <= rounds; r += 8) runLoads<8, ITEMS, MODE>(prog, r * P + lane, nl, P, k, A, ii, ss, rf);
+        if (r + 4 <= rounds) {
+            runLoads<4, ITEMS, MODE>(prog, r * P + lane, nl, P, k, A, ii, ss, rf);
+            r += 4;
         }
+        if (r + 2 <= rounds) {
+            runLoads<2, ITEMS, MODE>(prog, r * P + lane, nl, P, k, A, ii, ss, rf);
+            r += 2;
+        }
+        if (r < rounds) runLoads<1, ITEMS, MODE>(prog, r * P + lane, nl, P, k, A, ii, ss, rf);
         if (P > 1) __syncwarp();
         // Compute bundles.
         double acc[ITEMS];
