@@ -248,6 +248,30 @@ __device__ bool gridBarrier(BarrierState* bar, int* hostError, unsigned long lon
 }
 
 
+// Stores of G rounds of an OP_ST bundle: y[row * n + i] for this lane's
+// entries (a lane past the end stores the last entry's value again, to the
+// same place).  A single-entry bundle may store the accumulator.
+template <unsigned G, int ITEMS>
+__device__ __forceinline__ void runStores(const std::uint32_t* e, unsigned cnt, unsigned first, unsigned P,
+                                          const RegFile& rf, unsigned flags, const double (&acc)[ITEMS],
+                                          const DevKernel& k, const EvalArgs& A, const std::uint64_t (&ii)[ITEMS],
+                                          const unsigned (&ss)[ITEMS], const bool (&valid)[ITEMS]) {
+    std::uint32_t ee[G];
+    double v[G][ITEMS];
+#pragma unroll
+    for (unsigned u = 0; u < G; ++u) ee[u] = e[min(first + u * P, cnt - 1)];
+#pragma unroll
+    for (unsigned u = 0; u < G; ++u)
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j)
+            v[u][j] = (G == 1 && (flags & symgb::engine::H_A_ACC)) ? acc[j] : rf.at(field(ee[u], 0), j);
+#pragma unroll
+    for (unsigned u = 0; u < G; ++u)
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j)
+            if (valid[j]) A.xw[(k.yoff + (std::uint64_t)(ee[u] >> 8) * k.n + ii[j]) * A.S + ss[j]] = v[u][j];
+}
+
 // Load entries first, first + P, ..., first + (W - 1) P of the load section
 // (this lane's share of W rounds; entries past the end are skipped): all
 // index loads, then all gathers, then the register writes, so up to W x ITEMS
@@ -394,27 +418,16 @@ __device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t
                     }
                     break;
                 case OP_ST: {
-                    // Same rounds as runBundle; a lane past the end stores the
-                    // last entry's value again, to the same place.
-                    const std::uint64_t yoff = k.yoff, n = k.n;
+                    // Rounds of 4, 2 and 1 entries as in runBundle.
                     const unsigned rounds = (cnt + P - 1) / P;
-                    for (unsigned r = 0; r < rounds; r += GROUP) {
-                        std::uint32_t ee[GROUP];
-                        double v[GROUP][ITEMS];
-#pragma unroll
-                        for (unsigned u = 0; u < GROUP; ++u) ee[u] = e[min((r + u) * P + lane, cnt - 1)];
-#pragma unroll
-                        for (unsigned u = 0; u < GROUP; ++u)
-#pragma unroll
-                            for (int j = 0; j < ITEMS; ++j)
-                                v[u][j] = (cnt == 1 && (flags & H_A_ACC)) ? acc[j] : rf.at(field(ee[u], 0), j);
-#pragma unroll
-                        for (unsigned u = 0; u < GROUP; ++u)
-                            if (r + u < rounds)
-#pragma unroll
-                                for (int j = 0; j < ITEMS; ++j)
-                                    if (valid[j]) A.xw[(yoff + (std::uint64_t)(ee[u] >> 8) * n + ii[j]) * S + ss[j]] = v[u][j];
+                    unsigned r = 0;
+                    for (; r + GROUP <= rounds; r += GROUP)
+                        runStores<GROUP, ITEMS>(e, cnt, r * P + lane, P, rf, 0, acc, k, A, ii, ss, valid);
+                    if (r + 2 <= rounds) {
+                        runStores<2, ITEMS>(e, cnt, r * P + lane, P, rf, 0, acc, k, A, ii, ss, valid);
+                        r += 2;
                     }
+                    if (r < rounds) runStores<1, ITEMS>(e, cnt, r * P + lane, P, rf, flags, acc, k, A, ii, ss, valid);
                     break;
                 }
                 default: break;
