@@ -631,7 +631,15 @@ Program bundle(const Program& lin, int window) {
 Program compileTemplate(const symgb_kernel_desc& k, int math, int window) {
     Compiler c(k, math);
     Program linear = c.run();
-    return bundle(linear, window);
+    // A wide window can keep more than MAX_REGISTERS values live; narrower
+    // windows keep fewer (window 1 is the linear code's own order).
+    for (int w = window;; w /= 2) {
+        try {
+            return bundle(linear, w);
+        } catch (const std::runtime_error&) {
+            if (w <= 1) throw;
+        }
+    }
 }
 
 std::string disassemble(const Program& p) {

@@ -86,15 +86,17 @@ def single(args):
     tt = time.perf_counter()
     res = tuner.exhaustive(u, stream, flush, space=space, runs=max(3, args.steps // 2))
     t_batch = tuner.time_schedule(u, res.best, stream, flush, runs=args.steps) * 1e-6
-    # per-kernel launch shapes on the plain schedule, kept if faster
+    # per-kernel launch shapes (plain and levels schedules), kept if faster
     pk = tuner.tune_kernels(u, flush, reps=max(3, args.steps // 2))
-    plain_any = tuner.Sched("plain", 1, 128, 1)
-    t_pk = tuner.time_schedule(u, plain_any, stream, flush, runs=args.steps) * 1e-6
+    t_pk = {kind: tuner.time_schedule(u, tuner.PerKernel(kind), stream, flush, runs=args.steps) * 1e-6
+            for kind in ("plain", "levels")}
     tune_s = time.perf_counter() - tt
+    best_pk = min(t_pk, key=t_pk.get)
     chosen = f"{res.best}"
-    if t_pk < t_batch:
-        t_batch, chosen = t_pk, f"plain with per-kernel shapes {[list(x) for x in pk.shapes]}"
-        plain_any.apply(u)
+    if t_pk[best_pk] < t_batch:
+        t_batch = t_pk[best_pk]
+        chosen = f"{best_pk} with per-kernel shapes {[list(x) for x in pk.shapes]}"
+        tuner.PerKernel(best_pk).apply(u)
     else:
         for k in range(u.num_kernels):
             u.set_kernel_shape(k)
@@ -113,7 +115,8 @@ def single(args):
         "plain": {"ms_per_execute": t_plain * 1e3, "nnz_per_s": nnz / t_plain, "max_rel_err": err_plain,
                   "hbm_gbs": u.algorithmic_bytes(1) / t_plain / 1e9},
         "batched": {"schedule": chosen, "unit_wide_best": str(res.best), "unit_wide_ms": res.best_us * 1e-3,
-                    "per_kernel_plain_ms": t_pk * 1e3, "ms_per_execute": t_batch * 1e3, "nnz_per_s": nnz * S / t_batch,
+                    "per_kernel_plain_ms": t_pk["plain"] * 1e3, "per_kernel_levels_ms": t_pk["levels"] * 1e3,
+                    "ms_per_execute": t_batch * 1e3, "nnz_per_s": nnz * S / t_batch,
                     "max_rel_err": err_batch, "algorithmic_bytes": alg, "hbm_gbs": alg / t_batch / 1e9,
                     "hbm_frac": alg / t_batch / 1e9 / peak, "fp64_tflops": flops / t_batch / 1e12,
                     "fp64_frac": flops / t_batch / fp, "tuning_s": round(tune_s, 1), "schedules_timed": res.timed + pk.timed},
@@ -273,8 +276,8 @@ def kernels(args):
     stream = tuner.bind_stream(u)
     unitwide = tuner.exhaustive(u, stream, flush, runs=5)
     full = tuner.tune_kernels(u, flush, reps=5)
-    plain_tuned = tuner.time_schedule(u, tuner.Sched("plain", 1, 128, 1), stream, flush, runs=7)
-    levels_tuned = tuner.time_schedule(u, tuner.Sched("levels", 1, 128, 1), stream, flush, runs=7)
+    plain_tuned = tuner.time_schedule(u, tuner.PerKernel("plain"), stream, flush, runs=7)
+    levels_tuned = tuner.time_schedule(u, tuner.PerKernel("levels"), stream, flush, runs=7)
     learned = tuner.tune_kernels_with_model(u, model, S, flush, k_top=args.k, reps=5)
     learned_total = float(sum(full.table[sh][k] for k, sh in enumerate(learned.shapes) if sh in full.table))
     u.run()

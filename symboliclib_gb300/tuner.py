@@ -223,10 +223,25 @@ def _apply_shapes(unit: native.Unit, shapes) -> None:
         unit.set_kernel_shape(k, i, l, t)
 
 
+@dataclass(frozen=True)
+class PerKernel:
+    """A schedule kind run with the kernels' own launch shapes: tiles follow
+    each kernel's shape (no fixed tile size)."""
+    kind: str = "plain"
+
+    def apply(self, unit: native.Unit, math_mode: int = native.MATH_FAST, graph: int = 1) -> None:
+        k, depth = KINDS[self.kind]
+        unit.set_schedule(kind=k, math=math_mode, items_per_tile=0, use_graph=graph, fusion_depth=depth)
+
+    def __str__(self) -> str:
+        return f"{self.kind} with per-kernel shapes"
+
+
 def tune_kernels(unit: native.Unit, flush=None, shapes=None, reps: int = 5) -> KernelTuneResult:
     """Exhaustive per-kernel tuning: every kernel timed in every shape."""
     shapes = KERNEL_SHAPES if shapes is None else shapes
     t0 = time.perf_counter()
+    PerKernel("plain").apply(unit)
     nk = unit.num_kernels
     table = {}
     for sh in shapes:
@@ -261,6 +276,7 @@ def tune_kernels_with_model(unit: native.Unit, model: KernelCostModel, num_sets:
     """Times only each kernel's top-k proposed shapes (k passes of
     time_kernels, pass r putting every kernel in its r-th proposal)."""
     t0 = time.perf_counter()
+    PerKernel("plain").apply(unit)
     summaries = [program_summary(unit, k) for k in range(unit.num_kernels)]
     props = propose_kernel_shapes(model, unit, num_sets, k_top, summaries)
     nk = unit.num_kernels
