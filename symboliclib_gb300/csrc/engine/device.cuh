@@ -42,7 +42,7 @@ struct BarrierState {
 // the same launch); MODE_LIB adds the library operations (pow, sin, ...),
 // whose code needs many registers, so programs without them run a variant
 // with a smaller register footprint and higher occupancy.
-enum : int { LOAD_CACHED = 0, LOAD_L2 = 1, MODE_L2 = 1, MODE_LIB = 2 };
+enum : int { MODE_L2 = 1, MODE_LIB = 2 };
 
 struct EvalArgs {
     const DevKernel* ks;
@@ -66,9 +66,10 @@ namespace {
 
 using namespace symgb::engine;
 
-template <int LOAD>
+// Gather of x: through L2 only when other SMs write x during the launch.
+template <int L2_ONLY>
 __device__ __forceinline__ double loadX(const double* a) {
-    if (LOAD == LOAD_L2) return __ldcg(a);
+    if (L2_ONLY) return __ldcg(a);
     return __ldg(a);
 }
 
