@@ -102,9 +102,11 @@ struct Program {
 // Operations a bundle may gather from: the next `window` not yet scheduled
 // operations of the linear code (larger windows give larger bundles and more
 // live registers; a template that would need more than MAX_REGISTERS is
-// scheduled again with half the window).  128 against 64 on the GB300:
-// Neo-Hookean 10^3 70.1 -> 57.8 us, cloth 100^2 x 16 sets unchanged.
-constexpr int BUNDLE_WINDOW = 128;
+// scheduled again with half the window).  64 against 128 on the GB300: the
+// multi-pattern cloth batch 3.70 -> 3.38 ms and Neo-Hookean 15^3 x 4 sets
+// 252 -> 230 us faster with 64 (fewer registers, more resident items);
+// Neo-Hookean 10^3 x 1 set 70 -> 58 us faster with 128.
+constexpr int BUNDLE_WINDOW = 64;
 
 // Compiles one kernel template.  Throws std::runtime_error on templates the
 // engine cannot execute (unknown operations, more than MAX_REGISTERS live
