@@ -108,6 +108,72 @@ struct SqrtOp {
 struct RecOp {
     __device__ double operator()(double x, double, double) const { return __ddiv_rn(1.0, x); }
 };
+
+// Fast-mode division, reciprocal and square root (OP_FDIV, OP_FREC, OP_FSQRT;
+// exact mode keeps the IEEE operations above).  Each starts from the
+// hardware's approximate reciprocal or reciprocal square root (PTX
+// rcp.approx.ftz.f64 / rsqrt.approx.ftz.f64), refines it by Newton-Raphson
+// and ends with one correction step that uses the residual an FMA computes
+// exactly (P. Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Develop. 34(1), 1990; for the
+// square root the coupled iteration of Goldschmidt's method).  With a start
+// error e the result carries e^3 or less beside its final rounding, so it
+// stays within one unit in the last place for any e below 2^-18.  Operands
+// outside the exponent window where every intermediate is a normal finite
+// number (this includes zero, subnormal, infinite and NaN operands and
+// negative square-root arguments) take the IEEE operation instead, except a
+// zero dividend, whose quotient a * (1/b) is already exact.
+__device__ __forceinline__ double rcpApprox(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    return r;
+}
+__device__ __forceinline__ double rsqrtApprox(double x) {
+    double r;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    return r;
+}
+// Sign and biased exponent (12 bits).
+__device__ __forceinline__ unsigned signExp(double x) { return (unsigned)__double2hiint(x) >> 20; }
+// The IEEE operations for operands outside the window, out of line: inlined,
+// the compiler evaluates them beside the fast sequence and selects, which
+// costs the sum of both.
+__device__ __noinline__ double ieeeDiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __noinline__ double ieeeSqrt(double x) { return __dsqrt_rn(x); }
+
+struct FastDivOp {  // |a|, |b| in [2^-500, 2^501)
+    __device__ double operator()(double a, double b, double) const {
+        const double r0 = rcpApprox(b);
+        const double r = __fma_rn(r0, __fma_rn(-b, r0, 1.0), r0);
+        const double q0 = __dmul_rn(a, r);
+        double q = __fma_rn(r, __fma_rn(-b, q0, a), q0);
+        const bool zeroA = (((unsigned)__double2hiint(a) << 1) | (unsigned)__double2loint(a)) == 0u;
+        if (zeroA) q = q0;
+        if (__builtin_expect((signExp(b) & 0x7ffu) - 523u > 1000u || (!zeroA && (signExp(a) & 0x7ffu) - 523u > 1000u), 0))
+            q = ieeeDiv(a, b);
+        return q;
+    }
+};
+struct FastRecOp {  // |x| in [2^-1000, 2^1001)
+    __device__ double operator()(double x, double, double) const {
+        double r = rcpApprox(x);
+        r = __fma_rn(r, __fma_rn(-x, r, 1.0), r);
+        r = __fma_rn(r, __fma_rn(-x, r, 1.0), r);
+        if (__builtin_expect((signExp(x) & 0x7ffu) - 23u > 2000u, 0)) r = ieeeDiv(1.0, x);
+        return r;
+    }
+};
+struct FastSqrtOp {  // x in [2^-900, 2^901)
+    __device__ double operator()(double x, double, double) const {
+        const double y = rsqrtApprox(x);
+        double g = __dmul_rn(x, y);          // sqrt(x) (1 + e)
+        const double h = __dmul_rn(0.5, y);  // 1 / (2 sqrt(x)) (1 + e)
+        g = __fma_rn(g, __fma_rn(-g, h, 0.5), g);
+        g = __fma_rn(__fma_rn(-g, g, x), h, g);
+        if (__builtin_expect(signExp(x) - 123u > 1800u, 0)) g = ieeeSqrt(x);
+        return g;
+    }
+};
 template <int OPC>
 struct LibOp {  // CUDA's double-precision math library
     __device__ double operator()(double x, double y, double) const {
@@ -398,6 +464,9 @@ __device__ __forceinline__ void evalTile(const DevKernel& k, const std::uint64_t
                 case OP_MOV: runBundle<ITEMS, 1, GROUP>(e, cnt, rf, lane, P, flags, acc, MovOp{}); break;
                 case OP_SQRT: runBundle<ITEMS, 1, LONG_GROUP>(e, cnt, rf, lane, P, flags, acc, SqrtOp{}); break;
                 case OP_REC: runBundle<ITEMS, 1, LONG_GROUP>(e, cnt, rf, lane, P, flags, acc, RecOp{}); break;
+                case OP_FDIV: runBundle<ITEMS, 2, LONG_GROUP>(e, cnt, rf, lane, P, flags, acc, FastDivOp{}); break;
+                case OP_FSQRT: runBundle<ITEMS, 1, LONG_GROUP>(e, cnt, rf, lane, P, flags, acc, FastSqrtOp{}); break;
+                case OP_FREC: runBundle<ITEMS, 1, LONG_GROUP>(e, cnt, rf, lane, P, flags, acc, FastRecOp{}); break;
                 case OP_POW: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 2>(e, cnt, rf, lane, P, LibOp<OP_POW>{}); break;
                 case OP_SIN: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_SIN>{}); break;
                 case OP_COS: if (MODE & MODE_LIB) runBundleSerial<ITEMS, 1>(e, cnt, rf, lane, P, LibOp<OP_COS>{}); break;

@@ -301,7 +301,7 @@ private:
             case N_DIV: {
                 Val a = expr(kids_[j][0]);
                 Val b = expr(kids_[j][1]);
-                Val r = binary(OP_DIV, a, b);
+                Val r = binary(fast_ ? OP_FDIV : OP_DIV, a, b);
                 --prog_.stats.flops;
                 ++prog_.stats.divs;
                 return r;
@@ -312,12 +312,12 @@ private:
                 return r;
             }
             case N_SQRT: {
-                Val r = unary(OP_SQRT, expr(kids_[j][0]));
+                Val r = unary(fast_ ? OP_FSQRT : OP_SQRT, expr(kids_[j][0]));
                 ++prog_.stats.sqrts;
                 return r;
             }
             case N_REC: {
-                Val r = unary(OP_REC, expr(kids_[j][0]));
+                Val r = unary(fast_ ? OP_FREC : OP_REC, expr(kids_[j][0]));
                 ++prog_.stats.divs;
                 return r;
             }
@@ -398,7 +398,9 @@ struct LinOp {
     std::uint64_t lit = 0;  // OP_LDK
 };
 
-bool isBinary(int op) { return op == OP_ADD || op == OP_SUB || op == OP_MUL || op == OP_DIV || op == OP_POW; }
+bool isBinary(int op) {
+    return op == OP_ADD || op == OP_SUB || op == OP_MUL || op == OP_DIV || op == OP_FDIV || op == OP_POW;
+}
 bool isFma(int op) { return op == OP_FMA || op == OP_FMS || op == OP_FNMA || op == OP_FNMS; }
 
 std::vector<LinOp> parseLinear(const std::vector<std::uint64_t>& w) {
@@ -518,7 +520,8 @@ Program bundle(const Program& lin, int window) {
     const int nb = (int)bundles.size();
     auto viaBundle = [](int op) {  // operations the interpreter runs through runBundle
         return op == OP_LDK || op == OP_ADD || op == OP_SUB || op == OP_MUL || op == OP_DIV || op == OP_NEG ||
-               op == OP_MOV || op == OP_SQRT || op == OP_REC || isFma(op);
+               op == OP_MOV || op == OP_SQRT || op == OP_REC || op == OP_FDIV || op == OP_FSQRT || op == OP_FREC ||
+               isFma(op);
     };
     std::vector<int> useCount(nv, 0);
     for (int j = 0; j < n; ++j)
@@ -645,7 +648,8 @@ Program compileTemplate(const symgb_kernel_desc& k, int math, int window) {
 std::string disassemble(const Program& p) {
     static const char* names[NUM_OPCODES] = {"end", "ldx", "ldc", "ldk", "st", "add", "sub", "mul", "div",
                                              "neg", "sqrt", "rec", "fma", "sin", "cos", "tan", "asin", "acos",
-                                             "atan", "exp", "log", "pow", "mov", "fms", "fnma", "fnms"};
+                                             "atan", "exp", "log", "pow", "mov", "fms", "fnma", "fnms",
+                                             "fdiv", "fsqrt", "frec"};
     std::ostringstream os;
     for (std::uint64_t w : p.loads) {
         const int op = (int)(w & 0xff), d = (int)((w >> 8) & 0xff);

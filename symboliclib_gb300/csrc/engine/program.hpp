@@ -60,6 +60,9 @@ enum Opcode : std::uint8_t {
     OP_FMS = 23,   // r[a] * r[b] - r[c]
     OP_FNMA = 24,  // -(r[a] * r[b]) + r[c]
     OP_FNMS = 25,  // -(r[a] * r[b]) - r[c]
+    OP_FDIV = 26,  // r[a] / r[b], fast mode: refined hardware reciprocal, within one ulp
+    OP_FSQRT = 27, // sqrt(r[a]), fast mode
+    OP_FREC = 28,  // 1 / r[a], fast mode
     NUM_OPCODES
 };
 

@@ -2,7 +2,8 @@
 bit-identical): the smallest meshes (kernels of one or two instances),
 random expression plans including groups split after structure-hash
 collisions, subnormal and non-finite values, and a value-set count that is
-no multiple of a warp."""
+no multiple of a warp; fast mode's division and square root across
+magnitudes (within the fast-mode tolerance)."""
 import numpy as np
 import pytest
 
@@ -65,6 +66,44 @@ def test_subnormal_and_non_finite_values():
         ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, [v])[0]
         for kind in SCHEDULES:
             assert same_bits(run_exact(w, [v], kind)[0], ref), (what, kind)
+
+
+def test_fast_division_and_square_root_across_magnitudes():
+    """Fast mode divides and takes square roots by refining the hardware
+    approximation inside an exponent window and takes the IEEE operation
+    outside it.  Random expression plans (quotients a / (b*b + 1), roots
+    sqrt(a*a + b*b + 1)) on inputs outside the window, zero dividends of
+    either sign, overflowing squares, inf and NaN: the same non-finite results
+    as the oracle and the finite ones within the fast-mode tolerance."""
+    for seed in (3, 41):
+        w = native.Workload("random", 20000, seed)
+        x = w.inputs[0]
+        i = np.arange(len(x))
+        rng = np.random.default_rng(seed)
+        cases = {
+            "tiny (outside the window)": x * 2.0 ** -520,
+            "subnormal": x * 1e-310,
+            "huge (squares overflow)": x * 1e200,
+            "signed zeros": np.where(i % 5 == 0, 0.0, np.where(i % 7 == 0, -0.0, x)),
+            "inf and nan": np.where(i % 17 == 3, -np.inf, np.where(i % 23 == 5, np.nan, x)),
+            "mixed magnitudes": x * 10.0 ** rng.uniform(-300, 300, len(x)),
+        }
+        for what, v in cases.items():
+            ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, [v])[0]
+            u = native.Unit.from_workload(w)
+            u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_FAST)
+            u.set_arg(0, v)
+            u.run()
+            out = u.get_result(0)
+            assert np.array_equal(np.isnan(out), np.isnan(ref)), (seed, what)
+            assert np.array_equal(np.isinf(out), np.isinf(ref)), (seed, what)
+            inf = np.isinf(ref)
+            assert np.array_equal(np.sign(out[inf]), np.sign(ref[inf])), (seed, what)
+            fin = np.isfinite(ref)
+            if fin.any():
+                a, r = out[fin], ref[fin]
+                floor = max(1e-10 * np.max(np.abs(r)), np.finfo(float).tiny)
+                assert np.max(np.abs(a - r) / np.maximum(np.abs(r), floor)) <= 1e-12, (seed, what)
 
 
 def test_value_sets_not_a_multiple_of_a_warp():
