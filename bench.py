@@ -101,7 +101,7 @@ class ClockSampler:
 # over the step's evalKernel launches, from one ncu capture of that exact
 # configuration on a GB300: (workload, size, sets, schedule, items, lanes,
 # threads per block) -> bytes.  Configurations not captured report null.
-MEASURED_TRAFFIC = {("cotan", 500, 1, "levels", 2, 1, 64): 82.3e6}
+MEASURED_TRAFFIC = {("cotan", 500, 1, "levels", 2, 1, 64): 82.45e6}
 
 
 def peaks():
@@ -342,8 +342,9 @@ def run_engine(args):
             "e2e": {"value": world * nnz * S / t_e2e, "unit": "nnz/s", "ms_per_step": t_e2e * 1e3,
                     "h2d_bytes_per_step": int(sum(a.nbytes for a in inputs)), "d2h_bytes_per_step": int(nnz * S * 8),
                     "max_rel_err_vs_fp64_model": e2e_err,
-                    "mode": "two units on two streams take alternate steps (async set_arg / run / get_result "
-                            "into pinned memory); every step copies its inputs in and its results out",
+                    "mode": "two units on two streams take alternate steps (async set_arg / run / get_result: "
+                            "results gathered on the device and copied to pinned memory on the unit's copy "
+                            "stream); every step copies its inputs in and its results out; no L2 flush",
                     "one_at_a_time": {"value": world * nnz * S / t_seq, "ms_per_step": t_seq * 1e3}},
             "clocks": clk.summary()}
     if not args.no_cpu_baseline:

@@ -182,10 +182,12 @@ int symgb_get_result_sets_device(symgb_unit_t u, double* d, int k);
 int symgb_synchronize(symgb_unit_t u);
 /* Asynchronous host transfers, for overlapping one execute's transfers with
  * another's evaluation: `d` must be page-locked host memory (cudaHostAlloc or
- * cudaHostRegister; anything else is SYMGB_ERR_ARGUMENT).  The input copy, or
- * the result gather written straight into `d`, is enqueued on the unit's
- * stream; `d` must not be touched before symgb_synchronize (or a later event
- * on that stream). */
+ * cudaHostRegister; anything else is SYMGB_ERR_ARGUMENT).  The input copy is
+ * enqueued on the unit's stream.  The result is gathered on the unit's stream
+ * into a device buffer and copied to `d` on the unit's own copy stream, which
+ * the unit's stream does not wait for (the next gather of the same container
+ * does).  `d` must not be touched before symgb_synchronize, which waits for
+ * both streams. */
 int symgb_set_arg_sets_async(symgb_unit_t u, const double* d, int i);
 int symgb_get_result_sets_async(symgb_unit_t u, double* d, int k);
 

@@ -487,6 +487,7 @@ int symgb_run_async(symgb_unit_t u) {
 int symgb_synchronize(symgb_unit_t u) {
     if (!u || !u->initialized) return fail(SYMGB_ERR_STATE, "synchronize before init");
     SYMGB_CUDA(cudaStreamSynchronize(u->stream));
+    if (u->copyStream) SYMGB_CUDA(cudaStreamSynchronize(u->copyStream));
     return checkDeviceError(u);
 }
 
@@ -588,12 +589,44 @@ int symgb_set_arg_sets_async(symgb_unit_t u, const double* d, int i) {
     return symgb_set_arg_sets_device(u, u->staging.ptr, i);
 }
 
+// The result is gathered on the unit's stream into a device buffer and copied
+// to the host by the copy engine on the unit's copy stream, which the unit's
+// stream does not wait for: the next execute's input copy and evaluation
+// overlap this one's result copy.  (Gathering straight into page-locked memory
+// would hold SMs for the whole transfer over the host link.)
 int symgb_get_result_sets_async(symgb_unit_t u, double* d, int k) {
     if (!u || !u->initialized) return fail(SYMGB_ERR_STATE, "get_result before init");
     if (k < 0 || (std::size_t)k >= u->outStart.size() || !d) return fail(SYMGB_ERR_ARGUMENT, "bad result index");
-    double* dd = mappedHost(d);
-    if (!dd) return fail(SYMGB_ERR_ARGUMENT, "async get_result needs page-locked memory");
-    return symgb_get_result_sets_device(u, dd, k);
+    if (!mappedHost(d)) return fail(SYMGB_ERR_ARGUMENT, "async get_result needs page-locked memory");
+    const std::size_t nk = u->outStart.size();
+    if (!u->copyStream) {
+        SYMGB_CUDA(cudaStreamCreateWithFlags(&u->copyStream, cudaStreamNonBlocking));
+        SYMGB_CUDA(cudaEventCreateWithFlags(&u->gatherDone, cudaEventDisableTiming));
+        u->copyDone.assign(nk, nullptr);
+    }
+    if (u->asyncOutSets != u->numSets) {
+        SYMGB_CUDA(cudaStreamSynchronize(u->copyStream));  // copies may still read the old buffer
+        std::size_t total = 0;
+        for (std::size_t j = 0; j < nk; ++j) total += u->outLength[j];
+        SYMGB_CUDA(u->asyncOut.alloc(std::max<std::size_t>(1, total * (std::size_t)u->numSets)));
+        u->asyncOutSets = u->numSets;
+    }
+    std::size_t off = 0;
+    for (int j = 0; j < k; ++j) off += u->outLength[j];
+    off *= (std::size_t)u->numSets;
+    const std::size_t n = u->outLength[k] * (std::size_t)u->numSets;
+    double* buf = u->asyncOut.ptr + off;
+    if (u->copyDone[k]) {
+        SYMGB_CUDA(cudaStreamWaitEvent(u->stream, u->copyDone[k], 0));
+    } else {
+        SYMGB_CUDA(cudaEventCreateWithFlags(&u->copyDone[k], cudaEventDisableTiming));
+    }
+    if (int e = symgb_get_result_sets_device(u, buf, k)) return e;
+    SYMGB_CUDA(cudaEventRecord(u->gatherDone, u->stream));
+    SYMGB_CUDA(cudaStreamWaitEvent(u->copyStream, u->gatherDone, 0));
+    SYMGB_CUDA(cudaMemcpyAsync(d, buf, n * 8, cudaMemcpyDeviceToHost, u->copyStream));
+    SYMGB_CUDA(cudaEventRecord(u->copyDone[k], u->copyStream));
+    return SYMGB_OK;
 }
 
 int symgb_finish(symgb_unit_t u) {

@@ -71,6 +71,16 @@ struct symgb_unit {
     std::size_t smemOptin = 48 * 1024;  // max dynamic shared memory per block
     cudaStream_t ownStream = nullptr, stream = nullptr;
     DevBuf<double> x, c, staging, outBuf;
+    // Asynchronous result copies (symgb_get_result_sets_async): gathered into
+    // asyncOut (every output container, value sets included, at its own
+    // offset) on `stream`, copied to the host on copyStream; copyDone[k] marks
+    // the end of container k's last copy, which the next gather into that
+    // region waits for.
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t gatherDone = nullptr;
+    std::vector<cudaEvent_t> copyDone;
+    DevBuf<double> asyncOut;
+    int asyncOutSets = 0;
     DevBuf<std::uint32_t> p, ids;
     DevBuf<std::uint64_t> progs;
     DevBuf<DevKernel> devKernels;
@@ -103,6 +113,16 @@ struct symgb_unit {
     }
 
     void release() {
+        if (copyStream) cudaStreamSynchronize(copyStream);  // copies may still read asyncOut
+        for (cudaEvent_t e : copyDone)
+            if (e) cudaEventDestroy(e);
+        copyDone.clear();
+        if (gatherDone) cudaEventDestroy(gatherDone);
+        gatherDone = nullptr;
+        if (copyStream) cudaStreamDestroy(copyStream);
+        copyStream = nullptr;
+        asyncOut.reset();
+        asyncOutSets = 0;
         dropGraph();
         for (cudaEvent_t e : timingEvents) cudaEventDestroy(e);
         timingEvents.clear();

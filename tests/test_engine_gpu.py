@@ -196,6 +196,48 @@ def test_async_transfers_between_two_units():
     assert lib.symgb_get_result_sets_async(units[0][0].handle, page.ctypes.data, 0) == -1
 
 
+def test_async_results_of_consecutive_executes_stay_apart():
+    """The async result copy runs on the unit's copy stream while the unit's
+    stream goes on: with different inputs in every step, 2 then 3 value sets,
+    and one destination per step, every destination holds its own step's
+    results (exact mode, bit-identical to the oracle)."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    w = native.Workload("cloth", 6, 5)
+    lib = native.symgb()
+    rng = np.random.default_rng(11)
+    units = []
+    for _ in range(2):
+        u = native.Unit.from_workload(w)
+        u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_EXACT)
+        st = torch.cuda.Stream()
+        native.check(lib.symgb_set_stream(u.handle, C.c_void_p(st.cuda_stream)))
+        units.append(u)
+    nnz = len(w.numeric)
+    for sets in (2, 3):
+        for u in units:
+            u.set_num_sets(sets)
+        steps = []
+        for k in range(8):
+            per_set = [[a * (1.0 + 0.05 * rng.standard_normal(a.shape)) for a in w.inputs] for _ in range(sets)]
+            ins = [torch.from_numpy(np.concatenate([ps[i] for ps in per_set])).pin_memory()
+                   for i in range(len(w.inputs))]
+            out = torch.full((nnz * sets,), -1.0, dtype=torch.float64).pin_memory()
+            u = units[k % 2]
+            for i, a in enumerate(ins):
+                native.check(lib.symgb_set_arg_sets_async(u.handle, C.c_void_p(a.data_ptr()), i))
+            native.check(lib.symgb_run_async(u.handle))
+            native.check(lib.symgb_get_result_sets_async(u.handle, C.c_void_p(out.data_ptr()), 0))
+            steps.append((per_set, ins, out))
+        for u in units:
+            native.check(lib.symgb_synchronize(u.handle))
+        for per_set, _, out in steps:
+            got = out.numpy().reshape(sets, -1)
+            for s in range(sets):
+                ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, per_set[s])[0]
+                assert bits_equal(got[s], ref), (sets, s)
+
+
 def test_larger_cases_match_oracle():
     """Sizes beyond the fixtures: engine exact mode vs the CPU oracle."""
     for name, size, seed in [("cotan", 60, 5), ("ata", 30, 6), ("cloth", 12, 7)]:
