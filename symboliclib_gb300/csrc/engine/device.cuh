@@ -341,8 +341,8 @@ __device__ __forceinline__ void runStores(const std::uint32_t* e, unsigned cnt, 
 
 // Load entries first, first + P, ..., first + (W - 1) P of the load section
 // (this lane's share of W rounds; entries past the end are skipped): all
-// index loads, then all gathers, then the register writes, so up to W x ITEMS
-// independent loads are in flight.  x slots fit in 32 bits (checked when the
+// index loads, then all gathers, constant and literal reads, then the
+// register writes, so up to W x ITEMS independent loads are in flight.  x slots fit in 32 bits (checked when the
 // unit is created).
 template <int W, int ITEMS, int MODE>
 __device__ __forceinline__ void runLoads(const std::uint64_t* prog, unsigned first, unsigned nl, unsigned P,
@@ -361,6 +361,7 @@ __device__ __forceinline__ void runLoads(const std::uint64_t* prog, unsigned fir
         for (int j = 0; j < ITEMS; ++j)
             slot[u][j] = op == OP_LDX ? __ldg(k.p + ((unsigned)(w >> 16) & 0xffffu) * k.n + ii[j]) + imm : imm;
     }
+    const double* lit = reinterpret_cast<const double*>(prog + k.litoff);
     double v[W][ITEMS];
 #pragma unroll
     for (int u = 0; u < W; ++u)
@@ -371,6 +372,8 @@ __device__ __forceinline__ void runLoads(const std::uint64_t* prog, unsigned fir
                 v[u][j] = loadX<MODE & MODE_L2>(A.x + (std::uint64_t)slot[u][j] * A.S + ss[j]);
             else if (op == OP_LDC)
                 v[u][j] = __ldg(k.c + (std::uint64_t)slot[u][j] * k.n + ii[j]);
+            else if (op == OP_LDK)
+                v[u][j] = lit[slot[u][j]];
             else
                 v[u][j] = 0.0;
         }

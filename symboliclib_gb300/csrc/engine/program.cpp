@@ -449,7 +449,7 @@ std::vector<LinOp> parseLinear(const std::vector<std::uint64_t>& w) {
 
 // Schedules the linear code into bundles and assigns registers (see the
 // description of the program format).
-Program bundle(const Program& lin, int window) {
+Program bundle(const Program& lin, int window, int literalLoads) {
     const std::vector<LinOp> ops = parseLinear(lin.words);
     const int n = (int)ops.size();
     const int nl = (int)lin.loads.size();
@@ -480,13 +480,58 @@ Program bundle(const Program& lin, int window) {
             cur[L.d] = defOf[j];
         }
     }
+    // Literal loads of the load section: the `literalLoads` most read distinct
+    // literals become values nv0 .. nv - 1, loaded before any arithmetic; every
+    // read of one of their literal-load operations reads that value instead,
+    // and those operations are dropped.
+    const int nv0 = (int)producer.size();
+    std::vector<std::uint64_t> loadedLiterals;
+    std::vector<char> dropped(n, 0);
+    {
+        auto literalRead = [&](int v) { return v < nv0 && producer[v] >= 0 && ops[producer[v]].op == OP_LDK; };
+        std::unordered_map<std::uint64_t, int> reads;
+        for (int j = 0; j < n; ++j)
+            for (int s = 0; s < ops[j].nsrc; ++s)
+                if (literalRead(use[j][s])) ++reads[ops[producer[use[j][s]]].lit];
+        std::vector<std::pair<int, std::uint64_t>> order;
+        for (const auto& r : reads) order.push_back({r.second, r.first});
+        std::sort(order.begin(), order.end(), [](const auto& a, const auto& b) {
+            return a.first != b.first ? a.first > b.first : a.second < b.second;
+        });
+        if ((int)order.size() > literalLoads) order.resize(std::max(0, literalLoads));
+        std::unordered_map<std::uint64_t, int> valueOf;
+        for (const auto& o : order) {
+            valueOf[o.second] = (int)producer.size();
+            producer.push_back(-1);
+            loadedLiterals.push_back(o.second);
+        }
+        for (int j = 0; j < n; ++j)
+            for (int s = 0; s < ops[j].nsrc; ++s) {
+                const int v = use[j][s];
+                if (!literalRead(v)) continue;
+                const auto it = valueOf.find(ops[producer[v]].lit);
+                if (it == valueOf.end()) continue;
+                const auto d = std::find(deps[j].begin(), deps[j].end(), producer[v]);
+                if (d != deps[j].end()) deps[j].erase(d);
+                use[j][s] = it->second;
+            }
+        std::vector<int> readers(producer.size(), 0);
+        for (int j = 0; j < n; ++j)
+            for (int s = 0; s < ops[j].nsrc; ++s) ++readers[use[j][s]];
+        for (int j = 0; j < n; ++j)
+            if (ops[j].op == OP_LDK && readers[defOf[j]] == 0) dropped[j] = 1;
+    }
     const int nv = (int)producer.size();
 
     // List scheduling: among the next `window` unscheduled operations, take
     // every ready operation of the most frequent opcode as one bundle.
+    constexpr int NOWHERE = 1 << 30;  // bundle index of a dropped operation
     std::vector<int> bundleOf(n, -1);
+    for (int j = 0; j < n; ++j)
+        if (dropped[j]) bundleOf[j] = NOWHERE;
     std::vector<std::vector<int>> bundles;
     int frontier = 0;
+    while (frontier < n && bundleOf[frontier] >= 0) ++frontier;
     std::vector<std::vector<int>> byOp(NUM_OPCODES);
     while (frontier < n) {
         for (auto& v : byOp) v.clear();
@@ -564,10 +609,12 @@ Program bundle(const Program& lin, int window) {
         if (nregs >= MAX_REGISTERS) throw std::runtime_error("template needs more than 255 live values");
         return nregs++;
     };
-    for (int v = 0; v < nl; ++v) {
+    auto loadValue = [&](int v) {
         slot[v] = alloc();
         freeAfter[std::max(0, lastUse[v])].push_back(v);
-    }
+    };
+    for (int v = 0; v < nl; ++v) loadValue(v);
+    for (int v = nv0; v < nv; ++v) loadValue(v);
     Program out;
     out.stats = lin.stats;
     for (int b = 0; b < nb; ++b) {
@@ -585,11 +632,23 @@ Program bundle(const Program& lin, int window) {
     }
     out.registers = nregs;
 
-    for (int i = 0; i < nl; ++i)
-        out.loads.push_back((lin.loads[i] & ~0xff00ull) | ((std::uint64_t)slot[i] << 8));
-
     std::vector<std::uint64_t> literals;
     std::unordered_map<std::uint64_t, std::uint32_t> literalIndex;
+    auto literalOf = [&](std::uint64_t bits) {
+        auto it = literalIndex.find(bits);
+        if (it == literalIndex.end()) {
+            it = literalIndex.emplace(bits, (std::uint32_t)literals.size()).first;
+            literals.push_back(bits);
+        }
+        if (it->second >= ENTRY_FIELD_LIMIT) throw std::runtime_error("too many literals");
+        return it->second;
+    };
+    for (int i = 0; i < nl; ++i)
+        out.loads.push_back((lin.loads[i] & ~0xff00ull) | ((std::uint64_t)slot[i] << 8));
+    for (int t = 0; t < nv - nv0; ++t)
+        out.loads.push_back((std::uint64_t)OP_LDK | ((std::uint64_t)slot[nv0 + t] << 8) |
+                            ((std::uint64_t)literalOf(loadedLiterals[t]) << 32));
+
     for (int b = 0; b < nb; ++b) {
         const auto& B = bundles[b];
         const int op = ops[B[0]].op;
@@ -602,13 +661,7 @@ Program bundle(const Program& lin, int window) {
             if (op == OP_ST) {
                 e = (std::uint32_t)slot[use[j][0]] | (L.row << 8);
             } else if (op == OP_LDK) {
-                auto it = literalIndex.find(L.lit);
-                if (it == literalIndex.end()) {
-                    it = literalIndex.emplace(L.lit, (std::uint32_t)literals.size()).first;
-                    literals.push_back(L.lit);
-                }
-                if (it->second >= ENTRY_FIELD_LIMIT) throw std::runtime_error("too many literals");
-                e = (std::uint32_t)slot[defOf[j]] | (it->second << 8);
+                e = (std::uint32_t)slot[defOf[j]] | (literalOf(L.lit) << 8);
             } else {
                 e = (std::uint32_t)slot[defOf[j]];
                 for (int s = 0; s < L.nsrc; ++s) e |= (std::uint32_t)slot[use[j][s]] << (8 * (s + 1));
@@ -631,18 +684,23 @@ Program bundle(const Program& lin, int window) {
 
 }  // namespace
 
-Program compileTemplate(const symgb_kernel_desc& k, int math, int window) {
+Program compileTemplate(const symgb_kernel_desc& k, int math, int window, int literalLoads) {
     Compiler c(k, math);
     Program linear = c.run();
     // A wide window can keep more than MAX_REGISTERS values live; narrower
-    // windows keep fewer (window 1 is the linear code's own order).
-    for (int w = window;; w /= 2) {
-        try {
-            return bundle(linear, w);
-        } catch (const std::runtime_error&) {
-            if (w <= 1) throw;
+    // windows keep fewer (window 1 is the linear code's own order).  Literals
+    // loaded up front are live from the start: without them as the last resort.
+    for (int lits : {literalLoads, 0}) {
+        for (int w = window;; w /= 2) {
+            try {
+                return bundle(linear, w, lits);
+            } catch (const std::runtime_error&) {
+                if (w <= 1 && lits == 0) throw;
+                if (w <= 1) break;
+            }
         }
     }
+    throw std::runtime_error("template needs more than 255 live values");
 }
 
 std::string disassemble(const Program& p) {
@@ -654,10 +712,15 @@ std::string disassemble(const Program& p) {
     for (std::uint64_t w : p.loads) {
         const int op = (int)(w & 0xff), d = (int)((w >> 8) & 0xff);
         const std::int32_t imm = (std::int32_t)(w >> 32);
-        if (op == OP_LDX)
+        if (op == OP_LDX) {
             os << "ldx r" << d << " row" << ((w >> 16) & 0xffff) << " off" << imm << "\n";
-        else
+        } else if (op == OP_LDK) {
+            double v;
+            std::memcpy(&v, &p.words[p.literalOffset + (std::uint32_t)imm], 8);
+            os << "ldk r" << d << " " << v << "\n";
+        } else {
             os << "ldc r" << d << " crow" << imm << "\n";
+        }
     }
     for (std::size_t pc = 0; pc < p.words.size();) {
         const std::uint64_t h = p.words[pc++];

@@ -26,7 +26,7 @@
 namespace symgb {
 namespace engine {
 
-// Load-section word: op (bits 0-7), dst (8-15), imm (32-63), see OP_LDX/OP_LDC.
+// Load-section word: op (bits 0-7), dst (8-15), imm (32-63), see OP_LDX/OP_LDC/OP_LDK.
 // Compute bundle: header word (op bits 0-7, entry count bits 8-23, accumulator
 // flags bits 24-27), then the
 // 32-bit entries, two per word (entry 2q in the low half of word q).  Entry
@@ -37,7 +37,7 @@ enum Opcode : std::uint8_t {
     OP_END = 0,
     OP_LDX = 1,   // r[dst] = x[p[row * n + i] + off]; row = bits 16-31, off = imm (signed)
     OP_LDC = 2,   // r[dst] = c[row * n + i]; row = imm
-    OP_LDK = 3,   // r[d] = literal
+    OP_LDK = 3,   // r[d] = literal (load section: imm = its index in the literal table)
     OP_ST = 4,    // y[row * n + i] = r[a]
     OP_ADD = 5,
     OP_SUB = 6,   // r[a] - r[b]  (== r[a] + -(r[b]) exactly)
@@ -87,9 +87,11 @@ struct ProgramStats {
 };
 
 // A program has two sections.  `loads` holds every distinct gather (LDX) and
-// per-instance constant read (LDC) of the template, each loaded once into its
-// own register before any arithmetic, so the interpreter can issue them all
-// back to back.  `words` holds the compute bundles (arithmetic, literal loads
+// per-instance constant read (LDC) of the template, and its most used
+// distinct literals (LDK, up to LITERAL_LOADS), each loaded once into its own
+// register before any arithmetic, so the interpreter can issue them all back
+// to back (a literal so loaded takes one register and no compute entry,
+// instead of one literal-load entry and one register per use site).  `words` holds the compute bundles (arithmetic, literal loads
 // and output stores), an OP_END word, then the literal table (one double per
 // word) starting at word `literalOffset`.
 struct Program {
@@ -111,11 +113,17 @@ struct Program {
 // Neo-Hookean 10^3 x 1 set 70 -> 58 us faster with 128.
 constexpr int BUNDLE_WINDOW = 64;
 
+// Distinct literals loaded in the load section.  ComputeKernel templates use
+// few distinct literals (6-8 in the cloth and Neo-Hookean Hessians) at many
+// sites (185 literal loads in the largest cloth kernel).
+constexpr int LITERAL_LOADS = 32;
+
 // Compiles one kernel template.  Throws std::runtime_error on templates the
 // engine cannot execute (unknown operations, more than MAX_REGISTERS live
 // values).  Loads are deduplicated: a gather that the template reads several
 // times is loaded once; the value is the same, so results do not change.
-Program compileTemplate(const symgb_kernel_desc& k, int math, int window = BUNDLE_WINDOW);
+Program compileTemplate(const symgb_kernel_desc& k, int math, int window = BUNDLE_WINDOW,
+                        int literalLoads = LITERAL_LOADS);
 
 // Human-readable listing (tests and debugging).
 std::string disassemble(const Program& p);

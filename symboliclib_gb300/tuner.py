@@ -168,7 +168,7 @@ def tune_with_model(unit: native.Unit, model: CostModel, stream, flush=None, k: 
 KERNEL_SHAPES = [(i, l, t) for (i, l) in SHAPES for t in (64, 128, 256)]
 
 _OPNAMES = {5: "add", 6: "sub", 7: "mul", 8: "div", 9: "neg", 10: "sqrt", 11: "rec", 12: "fma", 23: "fma", 24: "fma",
-            25: "fma"}
+            25: "fma", 26: "div", 27: "sqrt", 28: "rec"}
 
 
 def program_summary(unit: native.Unit, k: int, math_mode: int = native.MATH_FAST) -> dict:

@@ -6,7 +6,7 @@ the interpreter's semantics (evalTile in symboliclib_gb300/csrc/engine/
 device.cuh):
 
 * load section: LDX r = x[p[row * n + i] + off] (u32 slot arithmetic),
-  LDC r = c[off * n + i];
+  LDC r = c[off * n + i], LDK r = literal table[off];
 * compute bundles: one header word (opcode bits 0-7, entry count 8-23, flags
   24-27), then 32-bit entries `d | a << 8 | b << 16 | c << 24`, two per word;
   no entry of a bundle reads another entry's result; LDK entries hold the
@@ -105,6 +105,12 @@ def run_kernel(words: np.ndarray, nl: int, x: np.ndarray, p: np.ndarray, c: np.n
     x; returns statistics (bundles, entries) of what it ran."""
     w = [int(v) for v in words]
     i = np.arange(n, dtype=np.int64)
+    # the literal table follows the END word
+    pc = nl
+    while w[pc] & 0xff != OP_END:
+        cnt = (w[pc] >> 8) & 0xffff
+        pc += 1 + (cnt + 1) // 2
+    lit = np.array(w[pc + 1:], dtype=np.uint64).view(np.float64)
     R: dict[int, np.ndarray] = {}
     for q in range(nl):
         op, d, imm = w[q] & 0xff, (w[q] >> 8) & 0xff, (w[q] >> 32) & 0xffffffff
@@ -114,14 +120,10 @@ def run_kernel(words: np.ndarray, nl: int, x: np.ndarray, p: np.ndarray, c: np.n
             R[d] = x[slot.astype(np.int64)].copy()
         elif op == OP_LDC:
             R[d] = c[imm * n + i].copy()
+        elif op == OP_LDK:
+            R[d] = np.full(n, lit[imm])
         else:
             raise ValueError(f"opcode {op} in the load section")
-    # the literal table follows the END word
-    pc = nl
-    while w[pc] & 0xff != OP_END:
-        cnt = (w[pc] >> 8) & 0xffff
-        pc += 1 + (cnt + 1) // 2
-    lit = np.array(w[pc + 1:], dtype=np.uint64).view(np.float64)
 
     acc = np.zeros(n)
     pc, bundles, entries = nl, 0, 0
