@@ -118,3 +118,34 @@ def test_model_catches_a_planted_program_error():
     ids = np.ascontiguousarray(w.out_index_data, np.uint32)
     s, n = int(d.output_start[0]), int(d.output_length[0])
     assert not np.array_equal(x[ids[s:s + n].astype(np.int64)], ref)
+
+
+@pytest.mark.parametrize("seed", range(100, 116))
+def test_random_plans_sweep(seed):
+    """Sixteen more random expression plans (shapes, shared blocks, sizes)."""
+    w = native.Workload("random", 500 + 97 * (seed % 7), seed)
+    ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
+    assert np.array_equal(model(w, w.inputs, native.MATH_EXACT).view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.parametrize("name,size", [("cloth", 4), ("neohookean", 2)])
+def test_literals_are_loaded_once(name, size):
+    """The templates' distinct literals are loaded once each in the load
+    section (in range of the literal table); no literal-load entries remain
+    among the compute bundles."""
+    w = native.Workload(name, size, 3)
+    u = Created(w)
+    seen = 0
+    for k in range(w.plan.contents.num_kernels):
+        for math_mode in (native.MATH_EXACT, native.MATH_FAST):
+            words, _, nl = pm.kernel_program(u.lib, u.h, k, math_mode)
+            w64 = [int(v) for v in words]
+            pc = nl
+            while w64[pc] & 0xff != pm.OP_END:
+                assert w64[pc] & 0xff != pm.OP_LDK
+                pc += 1 + (((w64[pc] >> 8) & 0xffff) + 1) // 2
+            table = len(w64) - (pc + 1)
+            lits = [v >> 32 for v in w64[:nl] if v & 0xff == pm.OP_LDK]
+            assert len(lits) == len(set(lits)) and all(i < table for i in lits)
+            seen += len(lits)
+    assert seen > 0
