@@ -450,7 +450,7 @@ std::vector<LinOp> parseLinear(const std::vector<std::uint64_t>& w) {
 // Schedules the linear code into bundles and assigns registers (see the
 // description of the program format).
 Program bundle(const Program& lin, int window, int literalLoads) {
-    const std::vector<LinOp> ops = parseLinear(lin.words);
+    std::vector<LinOp> ops = parseLinear(lin.words);
     const int n = (int)ops.size();
     const int nl = (int)lin.loads.size();
 
@@ -480,18 +480,81 @@ Program bundle(const Program& lin, int window, int literalLoads) {
             cur[L.d] = defOf[j];
         }
     }
+    // Negations folded into their readers, values unchanged: a + -x = a - x and
+    // -x + b = b - x (IEEE defines a - b as a + -b, and addition commutes),
+    // a - -x = a + x, and an FMA multiplicand or addend -x flips the FMA's sign
+    // (the interpreter computes FNMA and FMS as FMAs of negated operands).  A
+    // negation is dropped when every reader takes it.
+    std::vector<char> dropped(n, 0);
+    {
+        std::vector<std::vector<int>> readersOf(producer.size());
+        for (int j = 0; j < n; ++j)
+            for (int s = 0; s < ops[j].nsrc; ++s)
+                if (readersOf[use[j][s]].empty() || readersOf[use[j][s]].back() != j) readersOf[use[j][s]].push_back(j);
+        auto fmaFlags = [](int op) {
+            return op == OP_FNMA ? FMA_NEG_PRODUCT
+                   : op == OP_FMS ? FMA_NEG_ADDEND
+                   : op == OP_FNMS ? FMA_NEG_PRODUCT | FMA_NEG_ADDEND
+                                   : 0;
+        };
+        static const int fmaOf[4] = {OP_FMA, OP_FNMA, OP_FMS, OP_FNMS};
+        auto redirect = [&](int j, int from, int to) {  // j's dependency on `from` becomes one on `to`
+            const auto d = std::find(deps[j].begin(), deps[j].end(), from);
+            if (d != deps[j].end()) deps[j].erase(d);
+            if (to >= 0 && std::find(deps[j].begin(), deps[j].end(), to) == deps[j].end()) deps[j].push_back(to);
+        };
+        for (int g = 0; g < n; ++g) {
+            if (ops[g].op != OP_NEG || defOf[g] < 0) continue;
+            const int v = defOf[g], x = use[g][0];
+            const std::vector<int>& rs = readersOf[v];
+            bool ok = !rs.empty();
+            for (int j : rs) {
+                const LinOp& L = ops[j];
+                const bool at0 = use[j][0] == v, at1 = L.nsrc > 1 && use[j][1] == v;
+                if (L.op == OP_ADD)
+                    ok = ok && !(at0 && at1);
+                else if (L.op == OP_SUB)
+                    ok = ok && !at0;
+                else if (!isFma(L.op))
+                    ok = false;
+            }
+            if (!ok) continue;
+            for (int j : rs) {
+                LinOp& L = ops[j];
+                if (L.op == OP_ADD || L.op == OP_SUB) {
+                    if (L.op == OP_ADD && use[j][0] == v) {
+                        std::swap(L.src[0], L.src[1]);
+                        std::swap(use[j][0], use[j][1]);
+                    }
+                    L.op = L.op == OP_ADD ? OP_SUB : OP_ADD;
+                    use[j][1] = x;
+                } else {
+                    int flags = fmaFlags(L.op);
+                    for (int q = 0; q < 3; ++q)
+                        if (use[j][q] == v) {
+                            use[j][q] = x;
+                            flags ^= q < 2 ? FMA_NEG_PRODUCT : FMA_NEG_ADDEND;
+                        }
+                    L.op = fmaOf[flags];
+                }
+                redirect(j, g, producer[x]);
+                readersOf[x].push_back(j);
+            }
+            dropped[g] = 1;
+        }
+    }
+
     // Literal loads of the load section: the `literalLoads` most read distinct
     // literals become values nv0 .. nv - 1, loaded before any arithmetic; every
     // read of one of their literal-load operations reads that value instead,
     // and those operations are dropped.
     const int nv0 = (int)producer.size();
     std::vector<std::uint64_t> loadedLiterals;
-    std::vector<char> dropped(n, 0);
     {
         auto literalRead = [&](int v) { return v < nv0 && producer[v] >= 0 && ops[producer[v]].op == OP_LDK; };
         std::unordered_map<std::uint64_t, int> reads;
         for (int j = 0; j < n; ++j)
-            for (int s = 0; s < ops[j].nsrc; ++s)
+            for (int s = 0; !dropped[j] && s < ops[j].nsrc; ++s)
                 if (literalRead(use[j][s])) ++reads[ops[producer[use[j][s]]].lit];
         std::vector<std::pair<int, std::uint64_t>> order;
         for (const auto& r : reads) order.push_back({r.second, r.first});
@@ -506,7 +569,7 @@ Program bundle(const Program& lin, int window, int literalLoads) {
             loadedLiterals.push_back(o.second);
         }
         for (int j = 0; j < n; ++j)
-            for (int s = 0; s < ops[j].nsrc; ++s) {
+            for (int s = 0; !dropped[j] && s < ops[j].nsrc; ++s) {
                 const int v = use[j][s];
                 if (!literalRead(v)) continue;
                 const auto it = valueOf.find(ops[producer[v]].lit);
@@ -517,7 +580,7 @@ Program bundle(const Program& lin, int window, int literalLoads) {
             }
         std::vector<int> readers(producer.size(), 0);
         for (int j = 0; j < n; ++j)
-            for (int s = 0; s < ops[j].nsrc; ++s) ++readers[use[j][s]];
+            for (int s = 0; !dropped[j] && s < ops[j].nsrc; ++s) ++readers[use[j][s]];
         for (int j = 0; j < n; ++j)
             if (ops[j].op == OP_LDK && readers[defOf[j]] == 0) dropped[j] = 1;
     }
@@ -570,7 +633,7 @@ Program bundle(const Program& lin, int window, int literalLoads) {
     };
     std::vector<int> useCount(nv, 0);
     for (int j = 0; j < n; ++j)
-        for (int s = 0; s < ops[j].nsrc; ++s) ++useCount[use[j][s]];
+        for (int s = 0; !dropped[j] && s < ops[j].nsrc; ++s) ++useCount[use[j][s]];
     std::vector<std::uint32_t> headerFlags(nb, 0);
     std::vector<char> inAccOnly(nv, 0);
     for (int b = 0; b + 1 < nb; ++b) {
@@ -596,7 +659,8 @@ Program bundle(const Program& lin, int window, int literalLoads) {
     // load section) through its last reading bundle.
     std::vector<int> lastUse(nv, -1);
     for (int j = 0; j < n; ++j)
-        for (int s = 0; s < ops[j].nsrc; ++s) lastUse[use[j][s]] = std::max(lastUse[use[j][s]], bundleOf[j]);
+        for (int s = 0; !dropped[j] && s < ops[j].nsrc; ++s)
+            lastUse[use[j][s]] = std::max(lastUse[use[j][s]], bundleOf[j]);
     std::vector<std::vector<int>> freeAfter(nb + 1);
     std::vector<int> slot(nv, -1), pool;
     int nregs = 0;
