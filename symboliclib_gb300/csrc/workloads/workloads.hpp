@@ -804,6 +804,22 @@ NT applyShape(const RandomShape<double>& s, Leaf&& leaf) {
     return st.back();
 }
 
+// Sums of `terms` products literal_k * in[...], the same literals in every
+// output, so one kernel template holds `terms` distinct literals (more than a
+// program loads up front: the rest stay literal-load entries).
+template <class NT>
+std::vector<NT> literalSums(const std::vector<NT>& in, int outputs, int terms) {
+    const int m = (int)in.size();
+    std::vector<NT> out;
+    out.reserve(outputs);
+    for (int o = 0; o < outputs; ++o) {
+        NT s = NT(1.0 + 1.0 / 3.0) * in[(o * 13) % m];
+        for (int k = 1; k < terms; ++k) s = s + NT(1.0 + 0.125 * k + 1.0 / (k + 3)) * in[(o * 13 + k * 7) % m];
+        out.push_back(s);
+    }
+    return out;
+}
+
 template <class NT>
 std::vector<NT> randomExpressions(const std::vector<NT>& in, int outputs, std::uint64_t seed) {
     Rng rng(seed);

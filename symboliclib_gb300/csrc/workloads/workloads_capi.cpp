@@ -58,7 +58,8 @@ typedef struct Workload* symgbw_t;
 
 const char* symgbw_last_error(void) { return g_err.c_str(); }
 
-// workload: "ata" (side), "cotan" (side), "cloth" (side).  vector_width: 0 for
+// workload: "ata" (side), "cotan" (side), "cloth" (side), "neohookean" (cells
+// per side), "random" (outputs), "literals" (outputs).  vector_width: 0 for
 // the device layout, k > 0 for the reference CPU layout with SIMD width k.
 int symgbw_build(const char* name, int size, unsigned long long seed, int vector_width, int want_text, symgbw_t* out) {
     try {
@@ -115,6 +116,18 @@ int symgbw_build(const char* name, int size, unsigned long long seed, int vector
             pb.addContainer(out.data(), out.size());
             w->inputs.push_back(vals);
             w->numeric = randomExpressions(vals, size, seed);
+            w->outputs = out.size();
+        } else if (n == "literals") {
+            Rng rng(seed ^ 0x11ULL);
+            const int m = std::max(64, size / 4);
+            std::vector<double> vals(m);
+            for (auto& v : vals) v = rng.uniform(-1.0, 1.0);
+            auto VS = variables(vals.size(), 0);
+            auto out = literalSums(VS, size, 40);
+            pb.addContainer(VS.data(), VS.size());
+            pb.addContainer(out.data(), out.size());
+            w->inputs.push_back(vals);
+            w->numeric = literalSums(vals, size, 40);
             w->outputs = out.size();
         } else if (n == "neohookean") {
             TetMesh m = tetMesh(size);

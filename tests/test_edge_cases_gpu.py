@@ -1,5 +1,6 @@
 """Edge cases of the device path against the CPU oracle (exact mode,
-bit-identical): the smallest meshes (kernels of one or two instances),
+bit-identical): the smallest meshes (kernels of one or two instances), a
+template with more distinct literals than the load section takes,
 random expression plans including groups split after structure-hash
 collisions, subnormal and non-finite values, and a value-set count that is
 no multiple of a warp; fast mode's division and square root across
@@ -35,7 +36,8 @@ def run_exact(w, inputs, kind, sets=1):
     return u.get_result(0).reshape(sets, -1)
 
 
-@pytest.mark.parametrize("name,size", [("cotan", 2), ("cotan", 3), ("cloth", 2), ("ata", 2), ("neohookean", 1)])
+@pytest.mark.parametrize("name,size", [("cotan", 2), ("cotan", 3), ("cloth", 2), ("ata", 2), ("neohookean", 1),
+                                       ("literals", 300)])
 def test_smallest_meshes(name, size):
     w = native.Workload(name, size, 4)
     ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]

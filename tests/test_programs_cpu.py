@@ -66,7 +66,7 @@ def test_fast_programs_within_tolerance(name, size, seed):
 
 
 @pytest.mark.parametrize("name,size", [("cotan", 40), ("cloth", 12), ("ata", 40), ("neohookean", 3),
-                                       ("random", 3000)])
+                                       ("random", 3000), ("literals", 300)])
 def test_exact_programs_match_oracle_on_larger_plans(name, size):
     w = native.Workload(name, size, 9)
     ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
@@ -149,3 +149,23 @@ def test_literals_are_loaded_once(name, size):
             assert len(lits) == len(set(lits)) and all(i < table for i in lits)
             seen += len(lits)
     assert seen > 0
+
+
+def test_literals_beyond_the_load_section_cap():
+    """A template with 40 distinct literals: the 32 most read are loaded in the
+    load section, the other 8 stay literal-load entries; both modes agree with
+    the oracle."""
+    w = native.Workload("literals", 300, 3)
+    u = Created(w)
+    words, _, nl = pm.kernel_program(u.lib, u.h, 0, native.MATH_FAST)
+    w64 = [int(v) for v in words]
+    assert sum(1 for v in w64[:nl] if v & 0xff == pm.OP_LDK) == 32
+    pc, entries = nl, 0
+    while w64[pc] & 0xff != pm.OP_END:
+        if w64[pc] & 0xff == pm.OP_LDK:
+            entries += (w64[pc] >> 8) & 0xffff
+        pc += 1 + (((w64[pc] >> 8) & 0xffff) + 1) // 2
+    assert entries == 8
+    ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
+    assert np.array_equal(model(w, w.inputs, native.MATH_EXACT).view(np.uint64), ref.view(np.uint64))
+    assert rel_err(model(w, w.inputs, native.MATH_FAST), ref) <= 1e-12
