@@ -106,7 +106,10 @@ void parallelFor(std::size_t n, std::size_t grain, const std::function<void(std:
         fn(0, n);
         return;
     }
-    const std::size_t chunks = std::min<std::size_t>((std::size_t)pool().size() * 4, (n + grain - 1) / grain);
+    // Many small chunks, taken dynamically: per-item costs are uneven (the
+    // output blocks of a decomposition, which come last, cost the most), and a
+    // few large chunks left one thread with most of the work.
+    const std::size_t chunks = std::min<std::size_t>((std::size_t)pool().size() * 64, (n + grain - 1) / grain);
     pool().run(n, (n + chunks - 1) / chunks, fn);
 }
 

@@ -1,5 +1,6 @@
 // ComputeUnit planning: containers -> decomposition -> kernels -> execution
 // order -> memory layout and tables (reference src/ComputeUnit.cpp:172-451).
+#include <atomic>
 #include <cstring>
 #include <iomanip>
 #include <map>
@@ -9,6 +10,7 @@
 #include <unordered_map>
 
 #include "symgb/frontend.hpp"
+#include "symgb/parallel.hpp"
 #include "symgb/traverse.hpp"
 
 namespace symgb {
@@ -141,6 +143,11 @@ Plan PlanBuilder::build() {
     // Memory layout: x = [inputs | output and intermediate slots in kernel order].
     std::size_t variableDataSize = 0;
     std::unordered_map<hash_t, std::size_t> intermediatePositions;
+    {
+        std::size_t slots = 0;
+        for (auto& k : P.kernels) slots += k.outputVariableData().size();
+        intermediatePositions.reserve(slots);
+    }
     for (auto& k : P.kernels) {
         k.outputOffset = inputDataSize_ + variableDataSize;
         for (auto var : k.outputVariableData()) {
@@ -160,18 +167,36 @@ Plan PlanBuilder::build() {
         P.constantData.insert(P.constantData.end(), cd.begin(), cd.end());
     }
 
-    std::map<int, std::size_t> inputOffsets(inputOffsets_.begin(), inputOffsets_.end());
+    // Index table: every kernel's variable slots, filled in parallel (the maps
+    // are only read here).  An input group without an offset reads from 0.
+    const std::map<int, std::size_t> inputOffsets(inputOffsets_.begin(), inputOffsets_.end());
+    std::size_t indices = 0;
     for (auto& k : P.kernels) {
-        k.indexOffset = P.positionData.size();
-        for (auto& x : k.variableData()) {
-            if (x[1] == GLOBAL_INTERMEDIATE || x[1] == EXPLICIT_INTERMEDIATE) {
-                auto it = intermediatePositions.find(hashVariable(x));
-                if (it == intermediatePositions.end()) throw std::runtime_error("intermediate read before it is produced");
-                P.positionData.push_back((unsigned)(inputDataSize_ + it->second));
-            } else {
-                P.positionData.push_back((unsigned)(inputOffsets[x[1]] + x[0]));
+        k.indexOffset = indices;
+        indices += k.variableData().size();
+    }
+    P.positionData.resize(indices);
+    for (auto& k : P.kernels) {
+        const auto& vd = k.variableData();
+        unsigned* out = P.positionData.data() + k.indexOffset;
+        std::atomic<bool> missing{false};
+        parallelFor(vd.size(), 4096, [&](std::size_t b, std::size_t e) {
+            for (std::size_t i = b; i < e; ++i) {
+                const auto& x = vd[i];
+                if (x[1] == GLOBAL_INTERMEDIATE || x[1] == EXPLICIT_INTERMEDIATE) {
+                    auto it = intermediatePositions.find(hashVariable(x));
+                    if (it == intermediatePositions.end()) {
+                        missing = true;
+                        continue;
+                    }
+                    out[i] = (unsigned)(inputDataSize_ + it->second);
+                } else {
+                    auto it = inputOffsets.find(x[1]);
+                    out[i] = (unsigned)((it == inputOffsets.end() ? 0 : it->second) + x[0]);
+                }
             }
-        }
+        });
+        if (missing) throw std::runtime_error("intermediate read before it is produced");
     }
 
     std::size_t acc = 0;
@@ -188,6 +213,15 @@ Plan PlanBuilder::build() {
     }
     P.inputDataSize = inputDataSize_;
     P.numTotalMemory = inputDataSize_ + variableDataSize;
+
+    // The blocks' expressions are released in parallel (most of their nodes
+    // belong to one block; reference counts are atomic meanwhile).
+    {
+        Symbolic::ConcurrentRefs concurrent;
+        parallelFor(blocks.size(), 1024, [&](std::size_t b, std::size_t e) {
+            for (std::size_t i = b; i < e; ++i) blocks[i] = ExpressionBlock();
+        });
+    }
     return std::move(plan_);
 }
 
