@@ -211,33 +211,40 @@ std::vector<ExpressionBlock> decompose(const std::vector<Symbolic>& expr, unsign
         count[x.id()].second = (unsigned)nodes.size();
     }
 
-    // 3. Child links and node complexities.
-    for (auto& node : nodes) {
-        if (node.status == FIXED_NODE) {
-            node.complexity = 255;
-            continue;
+    // 3. Child links and node complexities.  Each node only reads the
+    // occurrence map and the expression graph and writes its own links, so the
+    // nodes are processed in parallel; parent counts are added afterwards.
+    parallelFor(nodes.size(), 64, [&](std::size_t b, std::size_t e) {
+        for (std::size_t ni = b; ni < e; ++ni) {
+            Node& node = nodes[ni];
+            if (node.status == FIXED_NODE) {
+                node.complexity = 255;
+                continue;
+            }
+            int comp = 0;
+            preOrderTraverse(node.fullx, [&](const Symbolic& y) {
+                if (y.op() == FIXED) {
+                    const auto* d = count.find(y[1].id());
+                    node.childs.insert({y[1].ahash(), nodes.data() + d->second - 1});
+                    return false;
+                }
+                if (y.complexity() < threshold) {
+                    comp += y.complexity();
+                    return false;
+                }
+                const auto* d = count.find(y.id());
+                if (d && d->second != 0 && y.ahash() != node.hash()) {
+                    node.childs.insert({y.ahash(), nodes.data() + d->second - 1});
+                    return false;
+                }
+                comp += std::max(1, (int)y.numChilds()) * opInfo(y.op()).cost;
+                return true;
+            });
+            node.complexity = (unsigned char)std::min(255, comp);
         }
-        int comp = 0;
-        preOrderTraverse(node.fullx, [&](const Symbolic& y) {
-            if (y.op() == FIXED) {
-                auto& d = count[y[1].id()];
-                node.addChild({y[1].ahash(), nodes.data() + d.second - 1});
-                return false;
-            }
-            if (y.complexity() < threshold) {
-                comp += y.complexity();
-                return false;
-            }
-            const auto& d = count[y.id()];
-            if (d.second != 0 && y.ahash() != node.hash()) {
-                node.addChild({y.ahash(), nodes.data() + d.second - 1});
-                return false;
-            }
-            comp += std::max(1, (int)y.numChilds()) * opInfo(y.op()).cost;
-            return true;
-        });
-        node.complexity = (unsigned char)std::min(255, comp);
-    }
+    });
+    for (auto& node : nodes)
+        for (auto& c : node.childs) ++c.second->numParents;
 
     // 4. Merge small and single-parent children, assign levels.  `reachable`
     // is a flag per node; nodes live in one array, so index order is the
