@@ -41,6 +41,15 @@ inline hash_t hashVector(const std::vector<T>& v) {
     return crc64(v.data(), sizeof(T) * v.size());
 }
 
+// The CRC above starts from 0 and has no final XOR, so it is linear over
+// GF(2): crc64(A || B) = crc64Shift(crc64(A), |B|) ^ crc64(B), where
+// crc64Shift(c, n) is the state reached from c by n zero bytes.
+std::uint64_t crc64Shift(std::uint64_t crc, std::uint64_t zeroBytes);
+
+// hashVector of a vector of hashes, with chunks of a long vector hashed in
+// parallel and combined in order; the same value as hashVector.
+hash_t hashVectorParallel(const std::vector<hash_t>& v);
+
 template <class T>
 inline hash_t hashValue(const T& v) {
     return crc64(&v, sizeof(T));

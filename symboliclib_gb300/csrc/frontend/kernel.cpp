@@ -43,7 +43,7 @@ struct Lockstep {
                 hs[i] = x[i]->ahash();
             }
         });
-        if (!x.empty()) h = hashVector(hs);
+        if (!x.empty()) h = hashVectorParallel(hs);
     }
     // Hash of the instances' algebraic hashes (reference ComputeKernel.cpp:14-20).
     void init() {
@@ -52,7 +52,7 @@ struct Lockstep {
         parallelFor(x.size(), kGrain, [&](std::size_t b, std::size_t e) {
             for (std::size_t i = b; i < e; ++i) hs[i] = x[i]->ahash();
         });
-        h = hashVector(hs);
+        h = hashVectorParallel(hs);
     }
     // True if any instance differs from the first in operation or child count.
     bool mixed() const {

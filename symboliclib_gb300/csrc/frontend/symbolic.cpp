@@ -7,6 +7,7 @@
 #include <mutex>
 #include <new>
 
+#include "symgb/parallel.hpp"
 #include "symgb/traverse.hpp"
 
 namespace symgb {
@@ -103,6 +104,62 @@ ChildPool& childPool() {
 const std::uint64_t* crc64Table() {
     static const Crc64Table table;
     return table.t;
+}
+
+namespace {
+
+// Zero-byte steps of the CRC as 64x64 matrices over GF(2), one per power of
+// two: column j of step[k] is the state that 2^k zero bytes make of bit j.
+struct Crc64Shifts {
+    std::uint64_t step[64][64];
+    static std::uint64_t apply(const std::uint64_t (&m)[64], std::uint64_t v) {
+        std::uint64_t r = 0;
+        for (int j = 0; v; ++j, v >>= 1)
+            if (v & 1) r ^= m[j];
+        return r;
+    }
+    Crc64Shifts() {
+        const std::uint64_t* tab = crc64Table();
+        for (int j = 0; j < 64; ++j) {
+            const std::uint64_t c = 1ULL << j;
+            step[0][j] = tab[(std::uint8_t)c] ^ (c >> 8);
+        }
+        for (int k = 1; k < 64; ++k)
+            for (int j = 0; j < 64; ++j) step[k][j] = apply(step[k - 1], step[k - 1][j]);
+    }
+};
+
+const Crc64Shifts& crc64Shifts() {
+    static const Crc64Shifts s;
+    return s;
+}
+
+}  // namespace
+
+std::uint64_t crc64Shift(std::uint64_t crc, std::uint64_t zeroBytes) {
+    const Crc64Shifts& s = crc64Shifts();
+    for (int k = 0; zeroBytes; ++k, zeroBytes >>= 1)
+        if (zeroBytes & 1) crc = Crc64Shifts::apply(s.step[k], crc);
+    return crc;
+}
+
+hash_t hashVectorParallel(const std::vector<hash_t>& v) {
+    constexpr std::size_t kChunk = 4096;  // hashes per chunk
+    if (v.size() < 4 * kChunk) return hashVector(v);
+    const std::size_t chunks = (v.size() + kChunk - 1) / kChunk;
+    std::vector<std::uint64_t> part(chunks);
+    parallelFor(chunks, 1, [&](std::size_t b, std::size_t e) {
+        for (std::size_t i = b; i < e; ++i) {
+            const std::size_t n = std::min(kChunk, v.size() - i * kChunk);
+            part[i] = (std::uint64_t)crc64(v.data() + i * kChunk, n * sizeof(hash_t));
+        }
+    });
+    std::uint64_t crc = 0;
+    for (std::size_t i = 0; i < chunks; ++i) {
+        const std::size_t n = std::min(kChunk, v.size() - i * kChunk);
+        crc = crc64Shift(crc, n * sizeof(hash_t)) ^ part[i];
+    }
+    return (hash_t)crc;
 }
 
 long long liveNodeCount() {

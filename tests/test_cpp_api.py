@@ -1,6 +1,7 @@
 """The C++ API (include/symgb/ComputeUnit.hpp, differentiation.hpp) compiled
 into a program: the reference Tutorial's known answers on the CPU, and a
-ComputeUnit compile/execute/getResults round trip on the GPU."""
+ComputeUnit compile/execute/getResults round trip on the GPU; the front end's
+parallel CRC-64 vector hash against the serial one."""
 import subprocess
 from pathlib import Path
 
@@ -30,4 +31,14 @@ def test_tutorial_known_answers(tutorial_binary):
 @pytest.mark.gpu
 def test_compute_unit_round_trip(tutorial_binary):
     r = subprocess.run([str(tutorial_binary), "--gpu"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_parallel_vector_hash_equals_serial():
+    out = build.OBJ / "crc_combine_test"
+    lib = build.LIB
+    cmd = ["g++", "-std=c++17", "-O1", f"-I{ROOT / 'include'}", str(ROOT / "tests" / "cpp" / "crc_combine.cpp"), "-o",
+           str(out), f"-L{lib}", "-lsymgb", f"-Wl,-rpath,{lib}"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    r = subprocess.run([str(out)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
