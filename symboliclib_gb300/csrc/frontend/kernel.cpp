@@ -76,17 +76,20 @@ struct Lockstep {
     // inverted and always fails.
     std::vector<std::array<int, 2>> variables() const {
         std::vector<std::array<int, 2>> v(x.size());
-        for (std::size_t i = 0; i < x.size(); ++i) v[i] = x[i]->variable();
+        parallelFor(x.size(), kGrain, [&](std::size_t b, std::size_t e) {
+            for (std::size_t i = b; i < e; ++i) v[i] = x[i]->variable();
+        });
         return v;
     }
     // The constant of every instance, or one value if all are equal.
     std::vector<double> constants() const {
         std::vector<double> v(x.size());
+        parallelFor(x.size(), kGrain, [&](std::size_t b, std::size_t e) {
+            for (std::size_t i = b; i < e; ++i) v[i] = x[i]->constant();
+        });
         bool allEqual = true;
-        for (std::size_t i = 0; i < x.size(); ++i) {
-            v[i] = x[i]->constant();
-            if (allEqual && v[0] != v[i]) allEqual = false;
-        }
+        for (std::size_t i = 1; i < v.size() && allEqual; ++i)
+            if (v[0] != v[i]) allEqual = false;
         if (allEqual) v.resize(1);
         return v;
     }

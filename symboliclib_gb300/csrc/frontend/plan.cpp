@@ -142,12 +142,9 @@ Plan PlanBuilder::build() {
 
     // Memory layout: x = [inputs | output and intermediate slots in kernel order].
     std::size_t variableDataSize = 0;
-    std::unordered_map<hash_t, std::size_t> intermediatePositions;
-    {
-        std::size_t slots = 0;
-        for (auto& k : P.kernels) slots += k.outputVariableData().size();
-        intermediatePositions.reserve(slots);
-    }
+    std::size_t slots = 0;
+    for (auto& k : P.kernels) slots += k.outputVariableData().size();
+    KeyMap<std::size_t> intermediatePositions(slots);  // sized up front: no rehashing
     for (auto& k : P.kernels) {
         k.outputOffset = inputDataSize_ + variableDataSize;
         for (auto var : k.outputVariableData()) {
@@ -184,12 +181,12 @@ Plan PlanBuilder::build() {
             for (std::size_t i = b; i < e; ++i) {
                 const auto& x = vd[i];
                 if (x[1] == GLOBAL_INTERMEDIATE || x[1] == EXPLICIT_INTERMEDIATE) {
-                    auto it = intermediatePositions.find(hashVariable(x));
-                    if (it == intermediatePositions.end()) {
+                    const std::size_t* pos = intermediatePositions.find(hashVariable(x));
+                    if (!pos) {
                         missing = true;
                         continue;
                     }
-                    out[i] = (unsigned)(inputDataSize_ + it->second);
+                    out[i] = (unsigned)(inputDataSize_ + *pos);
                 } else {
                     auto it = inputOffsets.find(x[1]);
                     out[i] = (unsigned)((it == inputOffsets.end() ? 0 : it->second) + x[0]);
