@@ -1,6 +1,7 @@
 """CPU tests of the C ABI boundary: every symbol declared in include/symgb.h is
-exported by the library, plans compile into device programs on the host, and
-invalid plans are rejected with an error code instead of reaching a kernel."""
+exported by the library, plans compile into device programs on the host,
+invalid plans are rejected with an error code instead of reaching a kernel,
+and calls out of order or with unsupported shapes return error codes."""
 import ctypes as C
 import re
 from pathlib import Path
@@ -87,4 +88,32 @@ def test_schedule_validation():
     assert lib.symgb_set_num_sets(h, 0) == -1
     native.check(lib.symgb_set_num_sets(h, 5))
     assert lib.symgb_num_sets(h) == 5
+    lib.symgb_unit_destroy(h)
+
+
+def test_calls_before_init_and_bad_kernel_shapes_are_errors():
+    """Host-side checks only: transfers, synchronisation and kernel timing
+    before init are state errors, and kernel shapes outside the supported set
+    are argument errors (no device call is reached)."""
+    w = native.Workload("cloth", 3, 31)
+    lib = native.symgb()
+    h = C.c_void_p()
+    native.check(lib.symgb_unit_create(w.plan, C.byref(h)))
+    buf = np.zeros(64)
+    assert lib.symgb_set_arg_sets_async(h, buf.ctypes.data, 0) == -3
+    assert lib.symgb_get_result_sets_async(h, buf.ctypes.data, 0) == -3
+    assert lib.symgb_set_arg_sets(h, buf.ctypes.data, 0) == -3
+    assert lib.symgb_get_result_sets(h, buf.ctypes.data, 0) == -3
+    assert lib.symgb_synchronize(h) == -3
+    us = (C.c_double * 64)()
+    assert lib.symgb_time_kernels(h, 1, None, 0, us) == -3
+    assert lib.symgb_time_kernels(h, 0, None, 0, us) == -1
+    nk = w.plan.contents.num_kernels
+    assert lib.symgb_set_kernel_shape(h, nk, 1, 1, 64) == -1       # no such kernel
+    assert lib.symgb_set_kernel_shape(h, 0, 3, 1, 64) == -1        # items per thread
+    assert lib.symgb_set_kernel_shape(h, 0, 1, 3, 64) == -1        # lanes per item
+    assert lib.symgb_set_kernel_shape(h, 0, 2, 2, 64) == -1        # lanes need one item
+    assert lib.symgb_set_kernel_shape(h, 0, 1, 1, 100) == -1       # not whole warps
+    native.check(lib.symgb_set_kernel_shape(h, 0, 1, 4, 128))
+    native.check(lib.symgb_set_kernel_shape(h, nk - 1, 0, 0, 0))   # back to the schedule's shape
     lib.symgb_unit_destroy(h)
