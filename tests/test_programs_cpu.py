@@ -169,3 +169,59 @@ def test_literals_beyond_the_load_section_cap():
     ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
     assert np.array_equal(model(w, w.inputs, native.MATH_EXACT).view(np.uint64), ref.view(np.uint64))
     assert rel_err(model(w, w.inputs, native.MATH_FAST), ref) <= 1e-12
+
+
+@pytest.mark.parametrize("name,size", [("cotan", 12), ("cloth", 6), ("ata", 12), ("neohookean", 2), ("random", 3000),
+                                       ("literals", 300)])
+def test_program_format_invariants(name, size):
+    """What the interpreter relies on, for every kernel in both modes: register
+    numbers below the program's register count (the shared-memory register
+    file is sized by it), no entry of a bundle reading or writing a register
+    that another entry of the same bundle writes (entries run in any order
+    across lanes), literal indices inside the literal table, accumulator flags
+    only on single-entry bundles, and every output row of the kernel stored."""
+    w = native.Workload(name, size, 5)
+    u = Created(w)
+    d = w.plan.contents
+    for k in range(d.num_kernels):
+        for math_mode in (native.MATH_EXACT, native.MATH_FAST):
+            words, regs, nl = pm.kernel_program(u.lib, u.h, k, math_mode)
+            w64 = [int(v) for v in words]
+            pc = nl
+            while w64[pc] & 0xff != pm.OP_END:
+                pc += 1 + (((w64[pc] >> 8) & 0xffff) + 1) // 2
+            table = len(w64) - (pc + 1)
+            assert 0 < regs <= 255
+            for v in w64[:nl]:
+                op, dst, imm = v & 0xff, (v >> 8) & 0xff, v >> 32
+                assert op in (pm.OP_LDX, pm.OP_LDC, pm.OP_LDK) and dst < regs
+                if op == pm.OP_LDK:
+                    assert imm < table
+            stored = set()
+            pc = nl
+            while w64[pc] & 0xff != pm.OP_END:
+                h = w64[pc]
+                op, cnt, flags = h & 0xff, (h >> 8) & 0xffff, h & 0xff000000
+                ents = [(w64[pc + 1 + q // 2] >> (32 * (q & 1))) & 0xffffffff for q in range(cnt)]
+                pc += 1 + (cnt + 1) // 2
+                assert cnt >= 1
+                if flags & (pm.H_A_ACC | pm.H_B_ACC | pm.H_C_ACC | pm.H_NOSTORE):
+                    assert cnt == 1
+                if op == pm.OP_ST:
+                    for e in ents:
+                        assert (e & 0xff) < regs
+                        stored.add(e >> 8)
+                    continue
+                if op == pm.OP_LDK:
+                    assert all((e >> 8) < table for e in ents)
+                    writes = [e & 0xff for e in ents]
+                    reads = []
+                else:
+                    writes = [e & 0xff for e in ents]
+                    reads = [(e >> (8 * (s + 1))) & 0xff for e in ents for s in range(pm.nsrc(op))
+                             if not flags & (pm.H_A_ACC << s)]
+                assert all(r < regs for r in writes + reads)
+                if not flags & pm.H_NOSTORE:
+                    assert len(set(writes)) == len(writes)
+                    assert not set(writes) & set(reads)
+            assert stored == set(range(d.kernels[k].num_output_rows))
