@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--lanes", type=int, default=1, help="threads per work item (1, 2, 4, 8)")
     ap.add_argument("--tpb", type=int, default=64, help="threads per block")
     ap.add_argument("--math", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--executor", default="compiled", choices=["compiled", "interpreter"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-probe", action="store_true", help="skip the FP64 peak probe (e.g. under a profiler)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -203,9 +204,12 @@ def run_engine(args):
     u = native.Unit.from_workload(w)
     stream = torch.cuda.Stream()
     native.check(native.symgb().symgb_set_stream(u.handle, C.c_void_p(stream.cuda_stream)))
+    execs = {"compiled": native.EXEC_COMPILED, "interpreter": native.EXEC_INTERPRETER}
     u.set_schedule(kind=kinds[args.schedule], math=native.MATH_FAST if args.math == "fast" else native.MATH_EXACT,
-                   threads_per_block=args.tpb, items_per_thread=args.items, lanes_per_item=args.lanes)
+                   threads_per_block=args.tpb, items_per_thread=args.items, lanes_per_item=args.lanes,
+                   executor=execs[args.executor])
     u.set_num_sets(S)
+    compile_s = u.prepare()
     inputs = [np.tile(a, S) for a in w.inputs]
     for i, a in enumerate(inputs):
         u.set_arg(i, a)
@@ -264,7 +268,8 @@ def run_engine(args):
     # unit's stream, so one step's transfers overlap the other's evaluation.
     u2 = native.Unit.from_workload(w)
     u2.set_schedule(kind=kinds[args.schedule], math=native.MATH_FAST if args.math == "fast" else native.MATH_EXACT,
-                    threads_per_block=args.tpb, items_per_thread=args.items, lanes_per_item=args.lanes)
+                    threads_per_block=args.tpb, items_per_thread=args.items, lanes_per_item=args.lanes,
+                    executor=execs[args.executor])
     u2.set_num_sets(S)
     stream2 = torch.cuda.Stream()
     native.check(lib.symgb_set_stream(u2.handle, C.c_void_p(stream2.cuda_stream)))
@@ -293,7 +298,8 @@ def run_engine(args):
     e2e_err = max(e2e_err, rel_err(pipe[1][2].numpy().reshape(S, -1)[0], w.numeric, 1e-4))
 
     # plain schedule (the reference's per-kernel launch structure) for comparison
-    u.set_schedule(kind=native.SCHEDULE_PLAIN, math=native.MATH_FAST)
+    u.set_schedule(kind=native.SCHEDULE_PLAIN, math=native.MATH_FAST, executor=execs[args.executor])
+    u.prepare()
     with torch.cuda.stream(stream):
         for _ in range(3):
             native.check(lib.symgb_run_async(u.handle))
@@ -323,7 +329,8 @@ def run_engine(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh)",
             "config": workload_config(args, w, {
-                "schedule": args.schedule, "items_per_thread": args.items, "lanes_per_item": args.lanes,
+                "schedule": args.schedule, "executor": args.executor, "compile_s": round(compile_s, 2),
+                "items_per_thread": args.items, "lanes_per_item": args.lanes,
                 "threads_per_block": args.tpb, "math": args.math, "l2": "flushed before every step (256 MiB write)",
                 "front_end_s": round(front_s, 2), "kernels": int(stats.num_kernels), "levels": int(stats.num_levels),
                 "max_rel_err_vs_fp64_model": err, "plain_schedule_ms_per_step": t_plain * 1e3,

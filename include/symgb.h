@@ -112,7 +112,45 @@ typedef struct symgb_schedule {
     int32_t lanes_per_item;     /* threads sharing one work item: 1, 2, 4 or 8 (0 = 1).  They
                                    split every bundle of the program and share the item's
                                    register file, which divides its shared memory per thread */
+    int32_t executor;           /* SYMGB_EXEC_*: how kernel templates run (below) */
 } symgb_schedule;
+
+/* Executors.  Both compute every value with the same operations in the same
+ * order, so their results are bit-identical in either math mode.
+ *   COMPILED: each template becomes straight-line CUDA C++ (the form of the
+ *     reference's generated kernels, ComputeUnit.cpp:409-421), one work item
+ *     per thread, compiled for sm_103a by NVRTC at the first run of a
+ *     configuration (math mode, value sets, schedule, block sizes) and cached
+ *     for the process; consecutive launches overlap their start-up
+ *     (programmatic dependent launch).  items_per_thread, lanes_per_item,
+ *     items_per_tile and fusion_depth do not apply.
+ *   INTERPRETER: one precompiled kernel runs every template as a bundled
+ *     register-machine program (no run-time compilation). */
+#define SYMGB_EXEC_COMPILED 0
+#define SYMGB_EXEC_INTERPRETER 1
+
+/* Compiles (or finds in the cache) the compiled executor's module for the
+ * unit's current schedule, value-set count and kernel shapes, so that a later
+ * run - or a graph capture, during which nothing may be compiled - does not
+ * pay for it.  *compile_seconds (if not NULL) receives the time this call
+ * spent (0 when cached).  No-op for the interpreter. */
+int symgb_prepare(symgb_unit_t u, double* compile_seconds);
+
+/* Host-only introspection of the compiled executor (no device needed): the
+ * generated CUDA C++ source of schedule `kind` (SYMGB_SCHEDULE_*) for the
+ * unit's current math mode, value sets and block sizes.  Writes up to `cap`
+ * bytes (NUL-terminated when it fits) and returns the source length, or a
+ * negative error.  symgb_compile_check compiles that source with NVRTC for
+ * sm_103a without loading it (the compile log is in symgb_last_error on
+ * failure) and reports the compile time. */
+int64_t symgb_compiled_source(symgb_unit_t u, int kind, char* buf, uint64_t cap);
+int symgb_compile_check(symgb_unit_t u, int kind, double* seconds);
+
+/* Failure-handling tests only: the limit of every bounded grid-barrier wait
+ * (default 2 s) and a number of arrivals each barrier waits for beyond the
+ * grid (default 0; > 0 makes every barrier wait out its limit, so the run
+ * returns SYMGB_ERR_TIMEOUT while the context stays usable). */
+int symgb_set_barrier_limits(symgb_unit_t u, uint64_t timeout_ns, int extra_arrivals);
 
 /* Launch shape of one kernel (items per thread, lanes per item, threads per
  * block; 0 = the schedule's value).  Used by the plain schedule for that

@@ -39,7 +39,8 @@ NVCCFLAGS = ARCH + ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-
                     "-Xptxas", "-warn-spills"]
 
 FRONTEND = sorted((CSRC / "frontend").glob("*.cpp"))
-ENGINE_CPP = [CSRC / "engine" / "program.cpp"]
+ENGINE_CPP = [CSRC / "engine" / "program.cpp", CSRC / "engine" / "codegen.cpp"]
+PRELUDE = CSRC / "engine" / "jit_prelude.cuh"
 ENGINE_CU = sorted((CSRC / "engine").glob("*.cu"))
 WORKLOADS = [CSRC / "workloads" / "workloads_capi.cpp"]
 ORACLE_SRC = [ROOT / "oracle" / "evaluate.c"]
@@ -76,22 +77,35 @@ def _compile(src: Path, force: bool, hdrs: list[Path]) -> Path:
     return out
 
 
+def _prelude_source() -> Path:
+    """The compiled executor's device prelude (jit_prelude.cuh) as a C++ string
+    constant, handed to NVRTC at the head of every generated module."""
+    out = OBJ / "jit_prelude_text.cpp"
+    text = PRELUDE.read_text()
+    body = ("namespace symgb {\nnamespace engine {\nextern const char* const kJitPrelude;\n"
+            f'const char* const kJitPrelude = R"SYMGB_PRELUDE({text})SYMGB_PRELUDE";\n}}\n}}\n')
+    if not out.exists() or out.read_text() != body:
+        out.write_text(body)
+    return out
+
+
 def build(force: bool = False, verbose: bool = False) -> dict[str, Path]:
     if not Path(NVCC).exists():
         raise RuntimeError(f"nvcc not found at {NVCC}")
     for d in (LIB, OBJ, ORACLE_BUILD):
         d.mkdir(parents=True, exist_ok=True)
     hdrs = _headers()
-    srcs = FRONTEND + ENGINE_CPP + ENGINE_CU + WORKLOADS + ORACLE_SRC
+    prelude = _prelude_source()
+    srcs = FRONTEND + ENGINE_CPP + [prelude] + ENGINE_CU + WORKLOADS + ORACLE_SRC
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         objs = dict(zip(srcs, ex.map(lambda s: _compile(s, force, hdrs), srcs)))
 
     cudalib = str(CUDA_HOME / "lib64")
     libsymgb = LIB / "libsymgb.so"
-    core = [objs[s] for s in FRONTEND + ENGINE_CPP + ENGINE_CU]
+    core = [objs[s] for s in FRONTEND + ENGINE_CPP + [prelude] + ENGINE_CU]
     if force or _stale(libsymgb, core):
         _run([NVCC] + ARCH + ["-shared", "-o", str(libsymgb)] + [str(o) for o in core]
-             + ["-lcudart", "-lpthread", f"-L{cudalib}", "-Xlinker", f"-rpath={cudalib}"])
+             + ["-lcudart", "-lnvrtc", "-lpthread", f"-L{cudalib}", "-Xlinker", f"-rpath={cudalib}"])
     libw = LIB / "libsymgb_workloads.so"
     wobjs = [objs[s] for s in WORKLOADS]
     if force or _stale(libw, wobjs + [libsymgb]):

@@ -53,7 +53,7 @@ struct EvalArgs {
     double* xw;
     unsigned S;
     unsigned progCap;               // program words that fit in shared memory (0: read from global)
-    unsigned reserved;
+    unsigned barrierExtra;          // arrivals beyond the grid a barrier waits for (timeout tests; 0)
     BarrierState* bar;
     int* hostError;
     unsigned long long timeoutNs;
@@ -73,10 +73,9 @@ __device__ __forceinline__ double loadX(const double* a) {
     return __ldg(a);
 }
 
-// Negation flips the sign bit (as C's unary minus does), on the integer pipe.
-__device__ __forceinline__ double negate(double x) {
-    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
-}
+#include "jit_prelude.cuh"
+
+__device__ __forceinline__ double negate(double x) { return symgbNegate(x); }
 
 struct AddOp {
     __device__ double operator()(double x, double y, double) const { return __dadd_rn(x, y); }
@@ -109,70 +108,15 @@ struct RecOp {
     __device__ double operator()(double x, double, double) const { return __ddiv_rn(1.0, x); }
 };
 
-// Fast-mode division, reciprocal and square root (OP_FDIV, OP_FREC, OP_FSQRT;
-// exact mode keeps the IEEE operations above).  Each starts from the
-// hardware's approximate reciprocal or reciprocal square root (PTX
-// rcp.approx.ftz.f64 / rsqrt.approx.ftz.f64), refines it by Newton-Raphson
-// and ends with one correction step that uses the residual an FMA computes
-// exactly (P. Markstein, "Computation of elementary functions on the IBM
-// RISC System/6000 processor", IBM J. Res. Develop. 34(1), 1990; for the
-// square root the coupled iteration of Goldschmidt's method).  With a start
-// error e the result carries e^3 or less beside its final rounding, so it
-// stays within one unit in the last place for any e below 2^-18.  Operands
-// outside the exponent window where every intermediate is a normal finite
-// number (this includes zero, subnormal, infinite and NaN operands and
-// negative square-root arguments) take the IEEE operation instead, except a
-// zero dividend, whose quotient a * (1/b) is already exact.
-__device__ __forceinline__ double rcpApprox(double x) {
-    double r;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-    return r;
-}
-__device__ __forceinline__ double rsqrtApprox(double x) {
-    double r;
-    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-    return r;
-}
-// Sign and biased exponent (12 bits).
-__device__ __forceinline__ unsigned signExp(double x) { return (unsigned)__double2hiint(x) >> 20; }
-// The IEEE operations for operands outside the window, out of line: inlined,
-// the compiler evaluates them beside the fast sequence and selects, which
-// costs the sum of both.
-__device__ __noinline__ double ieeeDiv(double a, double b) { return __ddiv_rn(a, b); }
-__device__ __noinline__ double ieeeSqrt(double x) { return __dsqrt_rn(x); }
-
-struct FastDivOp {  // |a|, |b| in [2^-500, 2^501)
-    __device__ double operator()(double a, double b, double) const {
-        const double r0 = rcpApprox(b);
-        const double r = __fma_rn(r0, __fma_rn(-b, r0, 1.0), r0);
-        const double q0 = __dmul_rn(a, r);
-        double q = __fma_rn(r, __fma_rn(-b, q0, a), q0);
-        const bool zeroA = (((unsigned)__double2hiint(a) << 1) | (unsigned)__double2loint(a)) == 0u;
-        if (zeroA) q = q0;
-        if (__builtin_expect((signExp(b) & 0x7ffu) - 523u > 1000u || (!zeroA && (signExp(a) & 0x7ffu) - 523u > 1000u), 0))
-            q = ieeeDiv(a, b);
-        return q;
-    }
+// Fast-mode division, reciprocal and square root (jit_prelude.cuh).
+struct FastDivOp {
+    __device__ double operator()(double a, double b, double) const { return symgbFastDiv(a, b); }
 };
-struct FastRecOp {  // |x| in [2^-1000, 2^1001)
-    __device__ double operator()(double x, double, double) const {
-        double r = rcpApprox(x);
-        r = __fma_rn(r, __fma_rn(-x, r, 1.0), r);
-        r = __fma_rn(r, __fma_rn(-x, r, 1.0), r);
-        if (__builtin_expect((signExp(x) & 0x7ffu) - 23u > 2000u, 0)) r = ieeeDiv(1.0, x);
-        return r;
-    }
+struct FastRecOp {
+    __device__ double operator()(double x, double, double) const { return symgbFastRec(x); }
 };
-struct FastSqrtOp {  // x in [2^-900, 2^901)
-    __device__ double operator()(double x, double, double) const {
-        const double y = rsqrtApprox(x);
-        double g = __dmul_rn(x, y);          // sqrt(x) (1 + e)
-        const double h = __dmul_rn(0.5, y);  // 1 / (2 sqrt(x)) (1 + e)
-        g = __fma_rn(g, __fma_rn(-g, h, 0.5), g);
-        g = __fma_rn(__fma_rn(-g, g, x), h, g);
-        if (__builtin_expect(signExp(x) - 123u > 1800u, 0)) g = ieeeSqrt(x);
-        return g;
-    }
+struct FastSqrtOp {
+    __device__ double operator()(double x, double, double) const { return symgbFastSqrt(x); }
 };
 template <int OPC>
 struct LibOp {  // CUDA's double-precision math library
@@ -273,47 +217,13 @@ __device__ __forceinline__ void runBundleSerial(const std::uint32_t* e, unsigned
     }
 }
 
-__device__ __forceinline__ unsigned long long globalTimerNs() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
+// Grid-wide barrier of the persistent and fused schedules (bounded wait,
+// jit_prelude.cuh).  `extra` raises the number of arrivals the barrier waits
+// for beyond the grid (only for testing the timeout path; 0 otherwise).
+__device__ __forceinline__ bool gridBarrier(BarrierState* bar, int* hostError, unsigned long long timeoutNs,
+                                            unsigned extra) {
+    return symgbGridBarrier(bar, hostError, timeoutNs, gridDim.x + extra);
 }
-
-// Grid-wide barrier for a cooperative launch.  The wait is bounded: after
-// `timeoutNs` the waiting block records SYMGB_ERR_TIMEOUT in bar->error and in
-// the host-mapped flag `hostError`, and leaves.  Every block checks bar->error
-// after each barrier and returns when it is set.
-__device__ bool gridBarrier(BarrierState* bar, int* hostError, unsigned long long timeoutNs) {
-    __syncthreads();
-    __shared__ int failed;
-    if (threadIdx.x == 0) {
-        volatile unsigned int* gen = &bar->generation;
-        volatile int* err = &bar->error;
-        const unsigned int g = *gen;
-        __threadfence();
-        if (atomicAdd(&bar->count, 1u) == gridDim.x - 1) {
-            atomicExch(&bar->count, 0u);
-            __threadfence();
-            atomicAdd(&bar->generation, 1u);
-        } else {
-            const unsigned long long t0 = globalTimerNs();
-            while (*gen == g) {
-                if (*err) break;
-                if (globalTimerNs() - t0 > timeoutNs) {
-                    atomicExch(&bar->error, SYMGB_ERR_TIMEOUT);
-                    *(volatile int*)hostError = SYMGB_ERR_TIMEOUT;
-                    break;
-                }
-                __nanosleep(100);
-            }
-        }
-        __threadfence();
-        failed = *err != 0;
-    }
-    __syncthreads();
-    return !failed;
-}
-
 
 // Stores of G rounds of an OP_ST bundle: y[row * n + i] for this lane's
 // entries (a lane past the end stores the last entry's value again, to the
@@ -549,7 +459,7 @@ __global__ void __maxnreg__(EvalRegs<ITEMS>::value) evalKernel(EvalArgs A) {
             evalTile<ITEMS, LANES, MODE>(k, prog, regs, t, A);
         }
         if (sg + 1 < A.segEnd)
-            if (!gridBarrier(A.bar, A.hostError, A.timeoutNs)) return;
+            if (!gridBarrier(A.bar, A.hostError, A.timeoutNs, A.barrierExtra)) return;
     }
 }
 

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -22,6 +23,7 @@
 #include <string>
 #include <vector>
 
+#include "codegen.hpp"
 #include "device.cuh"
 #include "kernels.hpp"
 #include "program.hpp"
@@ -192,10 +194,135 @@ const void* evalFunction(int items, int lanes, bool l2, bool lib) {
     return symgb::engine::evalKernelFor(items, lanes, (l2 ? MODE_L2 : 0) | (lib ? MODE_LIB : 0));
 }
 
+// ------------------------------------------------------------------ compiled executor
+
+// Module configuration of the compiled executor for schedule `kind`: block
+// sizes as the interpreter's (per-kernel shapes for plain launches, the
+// heaviest kernel's shape for a level, the schedule's for the persistent
+// kernel).
+JitConfig jitConfig(const symgb_unit* u, int kind) {
+    JitConfig c;
+    c.kind = kind == SYMGB_SCHEDULE_PLAIN ? JIT_PLAIN : kind == SYMGB_SCHEDULE_LEVELS ? JIT_LEVELS : JIT_PERSISTENT;
+    c.math = u->sched.math;
+    c.numSets = (unsigned)u->numSets;
+    for (std::size_t k = 0; k < u->kernels.size(); ++k) c.kernelTpb.push_back(u->shapeOf(k).tpb);
+    if (c.kind == JIT_PERSISTENT) {
+        c.levelTpb.assign(1, u->tpb());
+    } else {
+        c.levelTpb.assign((std::size_t)std::max(1, u->numLevels), u->tpb());
+        std::vector<double> most(c.levelTpb.size(), -1.0);
+        for (std::size_t k = 0; k < u->kernels.size(); ++k) {
+            const auto& d = u->kernels[k].desc;
+            const double work = (double)d.num_instances * (double)(d.num_nodes + 1);
+            if (d.level >= 0 && (std::size_t)d.level < most.size() && work > most[d.level]) {
+                most[d.level] = work;
+                c.levelTpb[d.level] = u->shapeOf(k).tpb;
+            }
+        }
+    }
+    return c;
+}
+
+std::string jitKeyOf(const JitConfig& c) {
+    std::string k = std::to_string(c.kind) + "/" + std::to_string(c.math) + "/" + std::to_string(c.numSets) + "/";
+    for (int t : c.kernelTpb) k += std::to_string(t) + ",";
+    k += "/";
+    for (int t : c.levelTpb) k += std::to_string(t) + ",";
+    return k;
+}
+
+// The compiled module of schedule `kind` in the unit's current configuration,
+// generated and compiled on first use.  `seconds` receives the compile time
+// (0 when the module was already loaded).
+int getModule(symgb_unit* u, int kind, std::shared_ptr<const JitModule>* out, double* seconds = nullptr) {
+    if (seconds) *seconds = 0.0;
+    const JitConfig cfg = jitConfig(u, kind);
+    const std::string key = jitKeyOf(cfg);
+    auto it = u->jitModules.find(key);
+    if (it != u->jitModules.end()) {
+        *out = it->second;
+        return SYMGB_OK;
+    }
+    std::vector<symgb_kernel_desc> descs;
+    for (const auto& k : u->kernels) descs.push_back(k.desc);
+    JitSource src;
+    try {
+        src = generateModule(descs, u->numLevels, cfg);
+    } catch (const std::exception& e) {
+        return fail(SYMGB_ERR_ARGUMENT, std::string("compiled executor: ") + e.what());
+    }
+    for (const JitLaunch& L : src.launches)
+        if (L.blocks > 0x7fffffffull) return fail(SYMGB_ERR_ARGUMENT, "compiled executor: grid too large");
+    std::string err;
+    std::shared_ptr<const JitModule> m;
+    const auto t0 = std::chrono::steady_clock::now();
+    if (int e = loadModule(src, &m, &err)) return fail(e, err);
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    u->jitModules[key] = m;
+    *out = m;
+    return SYMGB_OK;
+}
+
+// Enqueues one evaluation with the compiled executor.  Launches after the
+// first overlap their start-up with the previous launch (programmatic
+// dependent launch; each kernel waits for its predecessor before reading x).
+// With `kernelEvents`, runs the plain module without that overlap and
+// records an event before and after each kernel's launch.
+int enqueueCompiled(symgb_unit* u, const std::vector<cudaEvent_t>* kernelEvents) {
+    std::shared_ptr<const JitModule> m;
+    if (int e = getModule(u, kernelEvents ? SYMGB_SCHEDULE_PLAIN : u->sched.kind, &m)) return e;
+    const double* x = u->x.ptr;
+    double* xw = u->x.ptr;
+    const std::uint32_t* p = u->p.ptr;
+    const double* c = u->c.ptr;
+    BarrierState* bar = u->barrier.ptr;
+    int* hostError = u->errorDev;
+    unsigned long long timeoutNs = u->barrierTimeoutNs;
+    unsigned extra = u->barrierExtra;
+    void* args[] = {(void*)&x, (void*)&xw, (void*)&p, (void*)&c, (void*)&bar, (void*)&hostError, (void*)&timeoutNs,
+                    (void*)&extra};
+    int launches = 0;
+    for (std::size_t j = 0; j < m->launches.size(); ++j) {
+        const JitLaunch& L = m->launches[j];
+        cudaLaunchAttribute at[2];
+        unsigned na = 0;
+        unsigned grid = (unsigned)L.blocks;
+        if (L.cooperative) {
+            int perSm = 0;
+            SYMGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, m->kernels[j], L.tpb, 0));
+            if (perSm < 1) return fail(SYMGB_ERR_ARGUMENT, "persistent schedule: kernel does not fit on an SM");
+            if (u->sched.blocks_per_sm > 0) perSm = std::min(perSm, u->sched.blocks_per_sm);
+            grid = std::max(1u, std::min<unsigned>(grid, (unsigned)(perSm * u->smCount)));
+            at[na].id = cudaLaunchAttributeCooperative;
+            at[na].val.cooperative = 1;
+            ++na;
+        }
+        if (j > 0 && !kernelEvents) {
+            at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            at[na].val.programmaticStreamSerializationAllowed = 1;
+            ++na;
+        }
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3((unsigned)L.tpb);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = u->stream;
+        cfg.attrs = na ? at : nullptr;
+        cfg.numAttrs = na;
+        if (kernelEvents && L.kernel >= 0) SYMGB_CUDA(cudaEventRecord((*kernelEvents)[2 * L.kernel], u->stream));
+        SYMGB_CUDA(cudaLaunchKernelExC(&cfg, m->kernels[j], args));
+        if (kernelEvents && L.kernel >= 0) SYMGB_CUDA(cudaEventRecord((*kernelEvents)[2 * L.kernel + 1], u->stream));
+        ++launches;
+    }
+    u->launchesPerRun = launches;
+    return SYMGB_OK;
+}
+
 // Enqueues one evaluation on the unit's stream.  With `kernelEvents`, runs the
 // plain schedule whatever the unit's and records an event before and after
 // each kernel's launch (per-kernel timing).
 int enqueueRun(symgb_unit* u, const std::vector<cudaEvent_t>* kernelEvents = nullptr) {
+    if (u->compiledExec()) return enqueueCompiled(u, kernelEvents);
     if (int e = buildTiles(u)) return e;
     const int items = u->items();
     const int tpb = u->launchTpb();
@@ -207,7 +334,7 @@ int enqueueRun(symgb_unit* u, const std::vector<cudaEvent_t>* kernelEvents = nul
     A.x = u->x.ptr;
     A.xw = u->x.ptr;
     A.S = (unsigned)u->numSets;
-    A.reserved = 0;
+    A.barrierExtra = u->barrierExtra;
     A.bar = u->barrier.ptr;
     A.hostError = u->errorDev;
     A.timeoutNs = u->barrierTimeoutNs;
@@ -321,6 +448,10 @@ int runAsync(symgb_unit* u) {
     if (!u->initialized) return fail(SYMGB_ERR_STATE, "run before init");
     if (u->sched.use_graph) {
         if (!u->graphValid) {
+            if (u->compiledExec()) {  // nothing may be compiled or loaded during the capture
+                std::shared_ptr<const JitModule> m;
+                if (int e = getModule(u, u->sched.kind, &m)) return e;
+            }
             if (int e = buildTiles(u)) return e;
             // smem attributes must be set outside capture
             cudaGraph_t g;
@@ -656,6 +787,8 @@ int symgb_set_schedule(symgb_unit_t u, const symgb_schedule* s) {
         return fail(SYMGB_ERR_ARGUMENT, "lanes_per_item must be 1, 2, 4 or 8");
     if (s->lanes_per_item > 1 && s->items_per_thread > 1)
         return fail(SYMGB_ERR_ARGUMENT, "several lanes per item need one item per thread");
+    if (s->executor != SYMGB_EXEC_COMPILED && s->executor != SYMGB_EXEC_INTERPRETER)
+        return fail(SYMGB_ERR_ARGUMENT, "unknown executor");
     const bool mathChanged = s->math != u->sched.math;
     u->sched = *s;
     u->dropGraph();
@@ -678,6 +811,54 @@ int symgb_set_kernel_shape(symgb_unit_t u, int k, int items_per_thread, int lane
     u->kernelShape.resize(u->kernels.size(), symgb_unit::Shape{0, 0, 0});
     u->kernelShape[k] = symgb_unit::Shape{items_per_thread, lanes_per_item, threads_per_block};
     ++u->shapesVersion;
+    u->dropGraph();
+    return SYMGB_OK;
+}
+
+int symgb_prepare(symgb_unit_t u, double* compile_seconds) {
+    if (compile_seconds) *compile_seconds = 0.0;
+    if (!u) return fail(SYMGB_ERR_ARGUMENT, "null unit");
+    if (!u->compiledExec()) return SYMGB_OK;
+    std::shared_ptr<const JitModule> m;
+    return getModule(u, u->sched.kind, &m, compile_seconds);
+}
+
+int64_t symgb_compiled_source(symgb_unit_t u, int kind, char* buf, uint64_t cap) {
+    if (!u || kind < 0 || kind > 2) return fail(SYMGB_ERR_ARGUMENT, "bad unit or schedule kind");
+    std::vector<symgb_kernel_desc> descs;
+    for (const auto& k : u->kernels) descs.push_back(k.desc);
+    std::string src;
+    try {
+        src = generateModule(descs, u->numLevels, jitConfig(u, kind)).source;
+    } catch (const std::exception& e) {
+        return fail(SYMGB_ERR_ARGUMENT, std::string("compiled executor: ") + e.what());
+    }
+    if (buf && cap) {
+        const std::size_t n = std::min<std::size_t>(cap, src.size() + 1);
+        std::memcpy(buf, src.c_str(), n);
+    }
+    return (int64_t)src.size();
+}
+
+int symgb_compile_check(symgb_unit_t u, int kind, double* seconds) {
+    if (seconds) *seconds = 0.0;
+    if (!u || kind < 0 || kind > 2) return fail(SYMGB_ERR_ARGUMENT, "bad unit or schedule kind");
+    std::vector<symgb_kernel_desc> descs;
+    for (const auto& k : u->kernels) descs.push_back(k.desc);
+    std::string src, err;
+    try {
+        src = generateModule(descs, u->numLevels, jitConfig(u, kind)).source;
+    } catch (const std::exception& e) {
+        return fail(SYMGB_ERR_ARGUMENT, std::string("compiled executor: ") + e.what());
+    }
+    if (int e = compileOnly(src, seconds, &err)) return fail(e, err);
+    return SYMGB_OK;
+}
+
+int symgb_set_barrier_limits(symgb_unit_t u, uint64_t timeout_ns, int extra_arrivals) {
+    if (!u || timeout_ns == 0 || extra_arrivals < 0) return fail(SYMGB_ERR_ARGUMENT, "bad barrier limits");
+    u->barrierTimeoutNs = timeout_ns;
+    u->barrierExtra = (unsigned)extra_arrivals;
     u->dropGraph();
     return SYMGB_OK;
 }
@@ -802,6 +983,10 @@ int symgb_batch_create(symgb_unit_t* units, int n, int streams, symgb_batch_t* o
     for (int i = 0; i < n; ++i) {
         if (!units[i] || !units[i]->initialized) return fail(SYMGB_ERR_STATE, "batch unit not initialized");
         if (int e = buildTiles(units[i])) return e;  // no allocation may happen inside the capture
+        if (units[i]->compiledExec()) {               // nor any compilation or module load
+            std::shared_ptr<const JitModule> m;
+            if (int e = getModule(units[i], units[i]->sched.kind, &m)) return e;
+        }
         b->units.push_back(units[i]);
     }
     SYMGB_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));

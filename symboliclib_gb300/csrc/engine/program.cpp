@@ -389,15 +389,6 @@ private:
 
 // ------------------------------------------------------------------ bundling
 
-struct LinOp {
-    int op = OP_END;
-    int d = -1;             // register written in the linear code, -1 if none
-    int src[3] = {-1, -1, -1};
-    int nsrc = 0;
-    std::uint32_t row = 0;  // OP_ST
-    std::uint64_t lit = 0;  // OP_LDK
-};
-
 bool isBinary(int op) {
     return op == OP_ADD || op == OP_SUB || op == OP_MUL || op == OP_DIV || op == OP_FDIV || op == OP_POW;
 }
@@ -747,6 +738,13 @@ Program bundle(const Program& lin, int window, int literalLoads) {
 }
 
 }  // namespace
+
+std::vector<LinOp> linearCode(const symgb_kernel_desc& k, int math, std::vector<std::uint64_t>* loads) {
+    Compiler c(k, math);
+    Program linear = c.run();
+    if (loads) *loads = linear.loads;
+    return parseLinear(linear.words);
+}
 
 Program compileTemplate(const symgb_kernel_desc& k, int math, int window, int literalLoads) {
     Compiler c(k, math);

@@ -125,6 +125,24 @@ constexpr int LITERAL_LOADS = 32;
 Program compileTemplate(const symgb_kernel_desc& k, int math, int window = BUNDLE_WINDOW,
                         int literalLoads = LITERAL_LOADS);
 
+// One operation of a template's linear code (before bundling): the form the
+// code generator of the compiled executor reads.  Registers are the linear
+// code's (reused once a value is dead); `d` is -1 for stores.  FMA variants
+// carry their sign in the opcode (OP_FMA / OP_FMS / OP_FNMA / OP_FNMS).
+struct LinOp {
+    int op = OP_END;
+    int d = -1;             // register written, -1 if none
+    int src[3] = {-1, -1, -1};
+    int nsrc = 0;
+    std::uint32_t row = 0;  // OP_ST: output row
+    std::uint64_t lit = 0;  // OP_LDK: the literal's bits
+};
+
+// The linear code of a template and, in `loads`, its load section (OP_LDX /
+// OP_LDC words as in Program::loads).  Same operations, operands and rounding
+// as the device program compileTemplate bundles from it.
+std::vector<LinOp> linearCode(const symgb_kernel_desc& k, int math, std::vector<std::uint64_t>* loads);
+
 // Human-readable listing (tests and debugging).
 std::string disassemble(const Program& p);
 

@@ -216,7 +216,7 @@ extern "C" int symgb_run_static(symgb_unit_t u, const uint32_t* index_data, cons
         A.xw = x;
         A.S = 1;
         A.progCap = progCap;
-        A.reserved = 0;
+        A.barrierExtra = 0;
         A.bar = reinterpret_cast<BarrierState*>(base + oBar);
         A.hostError = reinterpret_cast<int*>(base + oBar + sizeof(BarrierState));
         A.timeoutNs = u->barrierTimeoutNs;

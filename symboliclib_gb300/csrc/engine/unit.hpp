@@ -7,9 +7,11 @@
 #include <array>
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
+#include "codegen.hpp"
 #include "device.cuh"
 #include "program.hpp"
 #include "symgb.h"
@@ -60,7 +62,7 @@ struct symgb_unit {
     std::uint64_t numTotalMemory = 0, numIndices = 0, numOutputValues = 0, numConstants = 0;
     int threadsPerBlock = 128;
     int numLevels = 0;
-    symgb_schedule sched{SYMGB_SCHEDULE_PLAIN, SYMGB_MATH_FAST, 0, 0, 0, 0, 1, 0, 1};
+    symgb_schedule sched{SYMGB_SCHEDULE_PLAIN, SYMGB_MATH_FAST, 0, 0, 0, 0, 1, 0, 1, SYMGB_EXEC_COMPILED};
     int numSets = 1;
     bool usesLibrary = false;  // some program calls pow, sin, ... (interpreter variant MODE_LIB)
 
@@ -100,9 +102,15 @@ struct symgb_unit {
     int tilesSets = -1, tilesItems = -1, tilesMath = -1;
     cudaGraphExec_t graph = nullptr;
     bool graphValid = false;
+    // Compiled executor: modules by configuration key (schedule kind, math,
+    // value sets, block sizes); `jit` is the current schedule's.
+    std::map<std::string, std::shared_ptr<const symgb::engine::JitModule>> jitModules;
+    std::shared_ptr<const symgb::engine::JitModule> jit;
+    std::string jitKey;
     int lastLaunches = 0;
     int launchesPerRun = 0;
     unsigned long long barrierTimeoutNs = 2000000000ull;
+    unsigned barrierExtra = 0;  // arrivals beyond the grid each barrier waits for (failure tests only)
 
     ~symgb_unit() { release(); }
 
@@ -148,6 +156,7 @@ struct symgb_unit {
     }
 
     int mathIndex() const { return sched.math == SYMGB_MATH_EXACT ? 0 : 1; }
+    bool compiledExec() const { return sched.executor == SYMGB_EXEC_COMPILED; }
     int tpb() const { return sched.threads_per_block > 0 ? sched.threads_per_block : threadsPerBlock; }
     int items() const { return sched.items_per_thread == 2 || sched.items_per_thread == 4 ? sched.items_per_thread : 1; }
     int lanes() const { return sched.lanes_per_item > 1 ? sched.lanes_per_item : 1; }

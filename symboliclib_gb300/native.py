@@ -12,6 +12,7 @@ LIB_DIR = Path(__file__).resolve().parent / "lib"
 
 SCHEDULE_PLAIN, SCHEDULE_LEVELS, SCHEDULE_PERSISTENT = 0, 1, 2
 MATH_EXACT, MATH_FAST = 0, 1
+EXEC_COMPILED, EXEC_INTERPRETER = 0, 1
 
 
 class Node(C.Structure):
@@ -37,7 +38,8 @@ class PlanDesc(C.Structure):
 class Schedule(C.Structure):
     _fields_ = [("kind", C.c_int32), ("math", C.c_int32), ("threads_per_block", C.c_int32),
                 ("items_per_tile", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32),
-                ("items_per_thread", C.c_int32), ("fusion_depth", C.c_int32), ("lanes_per_item", C.c_int32)]
+                ("items_per_thread", C.c_int32), ("fusion_depth", C.c_int32), ("lanes_per_item", C.c_int32),
+                ("executor", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -105,6 +107,10 @@ SYMGB_FUNCTIONS = {
     "symgb_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_float,
                                   C.POINTER(C.c_float)]),
     "symgb_mlp_destroy": (None, [C.c_void_p]),
+    "symgb_prepare": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "symgb_compiled_source": (C.c_int64, [C.c_void_p, C.c_int, C.c_char_p, C.c_uint64]),
+    "symgb_compile_check": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    "symgb_set_barrier_limits": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int]),
     "symgb_kernel_program": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]),
 }
@@ -304,14 +310,15 @@ class SparseSolver:
 class Unit:
     """One engine unit (device state for a plan), driven through the C ABI."""
 
-    def __init__(self, plan: C.POINTER(PlanDesc), index_data, out_index_data, const_data):
+    def __init__(self, plan: C.POINTER(PlanDesc), index_data, out_index_data, const_data, init: bool = True):
         lib = symgb()
         h = C.c_void_p()
         check(lib.symgb_unit_create(plan, C.byref(h)))
         self._lib, self.handle = lib, h
         self._tables = (np.ascontiguousarray(index_data, np.uint32), np.ascontiguousarray(out_index_data, np.uint32),
                         np.ascontiguousarray(const_data, np.float64))
-        check(lib.symgb_init(h, *(t.ctypes.data for t in self._tables)))
+        if init:  # device memory and table upload; host-only uses (sources, statistics) skip it
+            check(lib.symgb_init(h, *(t.ctypes.data for t in self._tables)))
         d = plan.contents
         self.kernel_instances = [int(d.kernels[k].num_instances) for k in range(d.num_kernels)]
         self.kernel_levels = [int(d.kernels[k].level) for k in range(d.num_kernels)]
@@ -319,14 +326,39 @@ class Unit:
         self.output_length = [int(d.output_length[i]) for i in range(d.num_outputs)]
 
     @classmethod
-    def from_workload(cls, w: Workload) -> "Unit":
-        return cls(w.plan, w.index_data, w.out_index_data, w.const_data)
+    def from_workload(cls, w: Workload, init: bool = True) -> "Unit":
+        return cls(w.plan, w.index_data, w.out_index_data, w.const_data, init=init)
 
     def set_schedule(self, kind=SCHEDULE_PLAIN, math=MATH_FAST, threads_per_block=0, items_per_tile=0,
-                     blocks_per_sm=0, use_graph=0, items_per_thread=1, fusion_depth=0, lanes_per_item=1) -> None:
+                     blocks_per_sm=0, use_graph=0, items_per_thread=1, fusion_depth=0, lanes_per_item=1,
+                     executor=EXEC_COMPILED) -> None:
         s = Schedule(kind, math, threads_per_block, items_per_tile, blocks_per_sm, use_graph, items_per_thread,
-                     fusion_depth, lanes_per_item)
+                     fusion_depth, lanes_per_item, executor)
         check(self._lib.symgb_set_schedule(self.handle, C.byref(s)))
+
+    def prepare(self) -> float:
+        """Compiles the compiled executor's module for the current schedule
+        (symgb_prepare); returns the seconds spent (0 when cached)."""
+        t = C.c_double()
+        check(self._lib.symgb_prepare(self.handle, C.byref(t)))
+        return t.value
+
+    def compiled_source(self, kind: int) -> str:
+        n = self._lib.symgb_compiled_source(self.handle, kind, None, 0)
+        if n < 0:
+            check(int(n))
+        buf = C.create_string_buffer(int(n) + 1)
+        self._lib.symgb_compiled_source(self.handle, kind, buf, n + 1)
+        return buf.value.decode()
+
+    def compile_check(self, kind: int) -> float:
+        """Compiles the generated module with NVRTC (no device); returns seconds."""
+        t = C.c_double()
+        check(self._lib.symgb_compile_check(self.handle, kind, C.byref(t)))
+        return t.value
+
+    def set_barrier_limits(self, timeout_ns: int, extra_arrivals: int = 0) -> None:
+        check(self._lib.symgb_set_barrier_limits(self.handle, timeout_ns, extra_arrivals))
 
     def set_num_sets(self, n: int) -> None:
         check(self._lib.symgb_set_num_sets(self.handle, n))
