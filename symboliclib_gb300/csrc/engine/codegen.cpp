@@ -149,28 +149,54 @@ void emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, int mat
     os << "}\n\n";
 }
 
+// Work items of kernel k for block `b0` (relative to the kernel's first
+// block): `items` per thread, consecutive threads on consecutive items in
+// each of the thread's rounds (coalesced), rounds unrolled so the items'
+// loads are in flight together.
+void emitItems(std::ostringstream& os, int k, std::uint64_t total, unsigned S, int tpb, int items, int l2,
+               const std::string& b0, const char* indent) {
+    os << indent << "const unsigned long long w0 = (" << b0 << ") * " << (std::uint64_t)tpb * items
+       << "ull + threadIdx.x;\n";
+    if (items > 1) os << indent << "#pragma unroll\n" << indent << "for (int j = 0; j < " << items << "; ++j) {\n";
+    else os << indent << "{\n" << indent << "    const int j = 0;\n";
+    os << indent << "    const unsigned long long w = w0 + (unsigned long long)j * " << tpb << "ull;\n"
+       << indent << "    if (w < " << u64(total) << ") symgbBody" << k << "<" << l2 << ">(x, xw, p, c, w / " << S
+       << "ull, (unsigned)(w % " << S << "ull));\n"
+       << indent << "}\n";
+}
+
+std::uint64_t blocksFor(std::uint64_t total, int tpb, int items) {
+    const std::uint64_t per = (std::uint64_t)tpb * items;
+    return (total + per - 1) / per;
+}
+
 // Dispatch of block `b` over the kernels of one launch (kernel-major block
 // ranges, each kernel's work items in consecutive blocks).
 void emitDispatch(std::ostringstream& os, const std::vector<int>& ks, const std::vector<symgb_kernel_desc>& descs,
-                  unsigned S, int tpb, int l2, const char* indent) {
+                  unsigned S, int tpb, int items, int l2, const char* indent) {
     std::uint64_t first = 0;
+    const std::string inner = std::string(indent) + "    ";
     for (std::size_t q = 0; q < ks.size(); ++q) {
         const int k = ks[q];
         const std::uint64_t total = descs[k].num_instances * S;
-        const std::uint64_t blocks = (total + tpb - 1) / tpb;
-        os << indent << (q ? "else " : "") << "if (b < " << u64(first + blocks) << ") {\n"
-           << indent << "    const unsigned long long w = (b - " << u64(first) << ") * " << tpb << "ull + threadIdx.x;\n"
-           << indent << "    if (w < " << u64(total) << ") symgbBody" << k << "<" << l2 << ">(x, xw, p, c, w / " << S
-           << "ull, (unsigned)(w % " << S << "ull));\n"
-           << indent << "}\n";
+        const std::uint64_t blocks = blocksFor(total, tpb, items);
+        os << indent << (q ? "else " : "") << "if (b < " << u64(first + blocks) << ") {\n";
+        emitItems(os, k, total, S, tpb, items, l2, "b - " + u64(first), inner.c_str());
+        os << indent << "}\n";
         first += blocks;
     }
 }
 
-std::uint64_t blocksOf(const std::vector<int>& ks, const std::vector<symgb_kernel_desc>& descs, unsigned S, int tpb) {
+std::uint64_t blocksOf(const std::vector<int>& ks, const std::vector<symgb_kernel_desc>& descs, unsigned S, int tpb,
+                       int items) {
     std::uint64_t b = 0;
-    for (int k : ks) b += (descs[k].num_instances * S + tpb - 1) / tpb;
+    for (int k : ks) b += blocksFor(descs[k].num_instances * S, tpb, items);
     return b;
+}
+
+int checkedItems(int items) {
+    if (items != 1 && items != 2 && items != 4) throw std::runtime_error("codegen: items per thread must be 1, 2 or 4");
+    return items;
 }
 
 }  // namespace
@@ -203,14 +229,13 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
             const std::uint64_t total = descs[k].num_instances * S;
             if (!total) continue;
             const int tpb = cfg.kernelTpb.at(k);
+            const int items = checkedItems(cfg.kernelItems.at(k));
             const std::string name = "symgb_k" + std::to_string(k);
             os << "extern \"C\" __global__ void __launch_bounds__(" << tpb << ") " << name << params << ") {\n"
-               << "    symgbDependencyWait();\n    symgbLaunchDependents();\n"
-               << "    const unsigned long long w = (unsigned long long)blockIdx.x * " << tpb
-               << "ull + threadIdx.x;\n"
-               << "    if (w < " << u64(total) << ") symgbBody" << k << "<0>(x, xw, p, c, w / " << S
-               << "ull, (unsigned)(w % " << S << "ull));\n}\n\n";
-            out.launches.push_back({name, (int)k, -1, (std::uint64_t)((total + tpb - 1) / tpb), tpb, false});
+               << "    symgbDependencyWait();\n    symgbLaunchDependents();\n";
+            emitItems(os, (int)k, total, S, tpb, items, 0, "(unsigned long long)blockIdx.x", "    ");
+            os << "}\n\n";
+            out.launches.push_back({name, (int)k, -1, blocksFor(total, tpb, items), tpb, items, false});
         }
     } else if (cfg.kind == JIT_LEVELS) {
         for (int L = 0; L < numLevels; ++L) {
@@ -220,16 +245,18 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
                 return descs[a].num_instances * (descs[a].num_nodes + 1) > descs[b].num_instances * (descs[b].num_nodes + 1);
             });
             const int tpb = cfg.levelTpb.at(L);
+            const int items = checkedItems(cfg.levelItems.at(L));
             const std::string name = "symgb_l" + std::to_string(L);
             os << "extern \"C\" __global__ void __launch_bounds__(" << tpb << ") " << name << params << ") {\n"
                << "    symgbDependencyWait();\n    symgbLaunchDependents();\n"
                << "    const unsigned long long b = blockIdx.x;\n";
-            emitDispatch(os, ks, descs, S, tpb, 0, "    ");
+            emitDispatch(os, ks, descs, S, tpb, items, 0, "    ");
             os << "}\n\n";
-            out.launches.push_back({name, -1, L, blocksOf(ks, descs, S, tpb), tpb, false});
+            out.launches.push_back({name, -1, L, blocksOf(ks, descs, S, tpb, items), tpb, items, false});
         }
     } else if (cfg.kind == JIT_PERSISTENT) {
         const int tpb = cfg.levelTpb.at(0);
+        const int items = checkedItems(cfg.levelItems.at(0));
         os << "struct SymgbBarrier { unsigned count; unsigned generation; int error; int pad; };\n";
         os << "extern \"C\" __global__ void __launch_bounds__(" << tpb << ") symgb_persistent" << params
            << ", SymgbBarrier* bar, int* hostError, unsigned long long timeoutNs, unsigned extra) {\n"
@@ -241,15 +268,15 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
             if (ks.empty()) continue;
             if (!firstLevel)
                 os << "    if (!symgbGridBarrier(bar, hostError, timeoutNs, gridDim.x + extra)) return;\n";
-            const std::uint64_t nb = blocksOf(ks, descs, S, tpb);
+            const std::uint64_t nb = blocksOf(ks, descs, S, tpb, items);
             most = std::max(most, nb);
             os << "    for (unsigned long long b = blockIdx.x; b < " << u64(nb) << "; b += gridDim.x) {\n";
-            emitDispatch(os, ks, descs, S, tpb, firstLevel ? 0 : 1, "        ");
+            emitDispatch(os, ks, descs, S, tpb, items, firstLevel ? 0 : 1, "        ");
             os << "    }\n";
             firstLevel = false;
         }
         os << "}\n\n";
-        out.launches.push_back({"symgb_persistent", -1, -1, most, tpb, true});
+        out.launches.push_back({"symgb_persistent", -1, -1, most, tpb, items, true});
     } else {
         throw std::runtime_error("codegen: unknown schedule");
     }

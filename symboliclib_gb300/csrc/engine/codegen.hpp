@@ -24,8 +24,10 @@ struct JitConfig {
     int kind = JIT_LEVELS;
     int math = SYMGB_MATH_FAST;
     unsigned numSets = 1;
-    std::vector<int> kernelTpb;  // per ComputeKernel (JIT_PLAIN)
-    std::vector<int> levelTpb;   // per level (JIT_LEVELS); [0] for JIT_PERSISTENT
+    std::vector<int> kernelTpb;    // per ComputeKernel (JIT_PLAIN)
+    std::vector<int> levelTpb;     // per level (JIT_LEVELS); [0] for JIT_PERSISTENT
+    std::vector<int> kernelItems;  // work items per thread, per ComputeKernel (JIT_PLAIN)
+    std::vector<int> levelItems;   // per level (JIT_LEVELS); [0] for JIT_PERSISTENT
 };
 
 // One launch of a module: entry name, ComputeKernel (plain) or level (levels)
@@ -36,6 +38,7 @@ struct JitLaunch {
     int level;
     std::uint64_t blocks;
     int tpb;
+    int items;  // work items per thread
     bool cooperative;  // persistent: grid capped at the co-resident maximum
 };
 

@@ -205,11 +205,16 @@ JitConfig jitConfig(const symgb_unit* u, int kind) {
     c.kind = kind == SYMGB_SCHEDULE_PLAIN ? JIT_PLAIN : kind == SYMGB_SCHEDULE_LEVELS ? JIT_LEVELS : JIT_PERSISTENT;
     c.math = u->sched.math;
     c.numSets = (unsigned)u->numSets;
-    for (std::size_t k = 0; k < u->kernels.size(); ++k) c.kernelTpb.push_back(u->shapeOf(k).tpb);
+    for (std::size_t k = 0; k < u->kernels.size(); ++k) {
+        c.kernelTpb.push_back(u->shapeOf(k).tpb);
+        c.kernelItems.push_back(u->shapeOf(k).items);
+    }
     if (c.kind == JIT_PERSISTENT) {
         c.levelTpb.assign(1, u->tpb());
+        c.levelItems.assign(1, u->items());
     } else {
         c.levelTpb.assign((std::size_t)std::max(1, u->numLevels), u->tpb());
+        c.levelItems.assign(c.levelTpb.size(), u->items());
         std::vector<double> most(c.levelTpb.size(), -1.0);
         for (std::size_t k = 0; k < u->kernels.size(); ++k) {
             const auto& d = u->kernels[k].desc;
@@ -217,6 +222,7 @@ JitConfig jitConfig(const symgb_unit* u, int kind) {
             if (d.level >= 0 && (std::size_t)d.level < most.size() && work > most[d.level]) {
                 most[d.level] = work;
                 c.levelTpb[d.level] = u->shapeOf(k).tpb;
+                c.levelItems[d.level] = u->shapeOf(k).items;
             }
         }
     }
@@ -228,6 +234,10 @@ std::string jitKeyOf(const JitConfig& c) {
     for (int t : c.kernelTpb) k += std::to_string(t) + ",";
     k += "/";
     for (int t : c.levelTpb) k += std::to_string(t) + ",";
+    k += "/";
+    for (int t : c.kernelItems) k += std::to_string(t) + ",";
+    k += "/";
+    for (int t : c.levelItems) k += std::to_string(t) + ",";
     return k;
 }
 

@@ -117,3 +117,15 @@ def test_calls_before_init_and_bad_kernel_shapes_are_errors():
     native.check(lib.symgb_set_kernel_shape(h, 0, 1, 4, 128))
     native.check(lib.symgb_set_kernel_shape(h, nk - 1, 0, 0, 0))   # back to the schedule's shape
     lib.symgb_unit_destroy(h)
+
+
+def test_barrier_limits_are_validated():
+    """symgb_set_barrier_limits (failure tests) rejects a zero limit, negative
+    extra arrivals and a null unit."""
+    w = native.Workload("cotan", 5, 21)
+    u = native.Unit.from_workload(w, init=False)
+    lib = native.symgb()
+    assert lib.symgb_set_barrier_limits(u.handle, 0, 0) == -1
+    assert lib.symgb_set_barrier_limits(u.handle, 1000, -1) == -1
+    assert lib.symgb_set_barrier_limits(None, 1000, 0) == -1
+    assert lib.symgb_set_barrier_limits(u.handle, 1000, 0) == 0

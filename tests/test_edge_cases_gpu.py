@@ -15,6 +15,7 @@ import oracle.cpu as ocpu
 pytestmark = pytest.mark.gpu
 
 SCHEDULES = [native.SCHEDULE_PLAIN, native.SCHEDULE_LEVELS, native.SCHEDULE_PERSISTENT]
+EXECUTORS = [native.EXEC_COMPILED, native.EXEC_INTERPRETER]
 
 
 def same_bits(a, b):
@@ -26,9 +27,9 @@ def same_bits(a, b):
     return bool(np.all(nan | (a.view(np.uint64) == b.view(np.uint64))))
 
 
-def run_exact(w, inputs, kind, sets=1):
+def run_exact(w, inputs, kind, sets=1, executor=native.EXEC_COMPILED):
     u = native.Unit.from_workload(w)
-    u.set_schedule(kind=kind, math=native.MATH_EXACT)
+    u.set_schedule(kind=kind, math=native.MATH_EXACT, executor=executor)
     u.set_num_sets(sets)
     for i, a in enumerate(inputs):
         u.set_arg(i, np.tile(a, sets))
@@ -41,8 +42,9 @@ def run_exact(w, inputs, kind, sets=1):
 def test_smallest_meshes(name, size):
     w = native.Workload(name, size, 4)
     ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
-    for kind in SCHEDULES:
-        assert same_bits(run_exact(w, w.inputs, kind)[0], ref), kind
+    for executor in EXECUTORS:
+        for kind in SCHEDULES:
+            assert same_bits(run_exact(w, w.inputs, kind, executor=executor)[0], ref), (kind, executor)
 
 
 @pytest.mark.parametrize("seed", [3, 22, 28, 41])
@@ -51,8 +53,9 @@ def test_random_expression_plans(seed):
     groups are split by structure before kernel construction."""
     w = native.Workload("random", 20000, seed)
     ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
-    for kind in SCHEDULES:
-        assert same_bits(run_exact(w, w.inputs, kind)[0], ref), kind
+    for executor in EXECUTORS:
+        for kind in SCHEDULES:
+            assert same_bits(run_exact(w, w.inputs, kind, executor=executor)[0], ref), (kind, executor)
 
 
 def test_subnormal_and_non_finite_values():
@@ -66,8 +69,9 @@ def test_subnormal_and_non_finite_values():
     }
     for what, v in cases.items():
         ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, [v])[0]
-        for kind in SCHEDULES:
-            assert same_bits(run_exact(w, [v], kind)[0], ref), (what, kind)
+        for executor in EXECUTORS:
+            for kind in SCHEDULES:
+                assert same_bits(run_exact(w, [v], kind, executor=executor)[0], ref), (what, kind, executor)
 
 
 def test_fast_division_and_square_root_across_magnitudes():
@@ -93,10 +97,14 @@ def test_fast_division_and_square_root_across_magnitudes():
         for what, v in cases.items():
             ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, [v])[0]
             u = native.Unit.from_workload(w)
-            u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_FAST)
-            u.set_arg(0, v)
-            u.run()
-            out = u.get_result(0)
+            outs = []
+            for executor in EXECUTORS:
+                u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_FAST, executor=executor)
+                u.set_arg(0, v)
+                u.run()
+                outs.append(u.get_result(0))
+            assert same_bits(outs[0], outs[1]), (seed, what)  # the same operations in both executors
+            out = outs[0]
             assert np.array_equal(np.isnan(out), np.isnan(ref)), (seed, what)
             assert np.array_equal(np.isinf(out), np.isinf(ref)), (seed, what)
             inf = np.isinf(ref)

@@ -18,6 +18,7 @@ import oracle.cpu as ocpu
 pytestmark = pytest.mark.gpu
 
 SCHEDULES = [native.SCHEDULE_PLAIN, native.SCHEDULE_LEVELS, native.SCHEDULE_PERSISTENT]
+EXECUTORS = [native.EXEC_COMPILED, native.EXEC_INTERPRETER]
 TOL = 1e-12
 FAST_FLOOR = {"cloth": 1e-4}
 
@@ -41,11 +42,12 @@ def bits_equal(a, b):
 
 @pytest.mark.parametrize("name,size,seed", GOLDEN_CASES)
 @pytest.mark.parametrize("kind", SCHEDULES)
-def test_exact_mode_bit_identical_to_reference(name, size, seed, kind):
+@pytest.mark.parametrize("executor", EXECUTORS)
+def test_exact_mode_bit_identical_to_reference(name, size, seed, kind, executor):
     _, inp, gold = load_golden(name, size)
     w = native.Workload(name, size, seed)
     u = native.Unit.from_workload(w)
-    u.set_schedule(kind=kind, math=native.MATH_EXACT)
+    u.set_schedule(kind=kind, math=native.MATH_EXACT, executor=executor)
     for i, a in enumerate(split_inputs(w, inp)):
         u.set_arg(i, a)
     u.run()
@@ -54,11 +56,12 @@ def test_exact_mode_bit_identical_to_reference(name, size, seed, kind):
 
 @pytest.mark.parametrize("name,size,seed", GOLDEN_CASES)
 @pytest.mark.parametrize("kind", SCHEDULES)
-def test_fast_mode_within_tolerance(name, size, seed, kind):
+@pytest.mark.parametrize("executor", EXECUTORS)
+def test_fast_mode_within_tolerance(name, size, seed, kind, executor):
     _, inp, gold = load_golden(name, size)
     w = native.Workload(name, size, seed)
     u = native.Unit.from_workload(w)
-    u.set_schedule(kind=kind, math=native.MATH_FAST)
+    u.set_schedule(kind=kind, math=native.MATH_FAST, executor=executor)
     for i, a in enumerate(split_inputs(w, inp)):
         u.set_arg(i, a)
     u.run()
@@ -68,12 +71,13 @@ def test_fast_mode_within_tolerance(name, size, seed, kind):
 @pytest.mark.parametrize("name,size,seed", [("cotan", 8, 22), ("cloth", 5, 32), ("ata", 9, 12)])
 @pytest.mark.parametrize("kind", SCHEDULES)
 @pytest.mark.parametrize("sets", [2, 7, 33, 64])
-def test_value_set_batches_match_oracle(name, size, seed, kind, sets):
+@pytest.mark.parametrize("executor", EXECUTORS)
+def test_value_set_batches_match_oracle(name, size, seed, kind, sets, executor):
     """S value sets in one run: every set bit-identical (exact mode) to the
     oracle evaluated on that set alone."""
     w = native.Workload(name, size, seed)
     u = native.Unit.from_workload(w)
-    u.set_schedule(kind=kind, math=native.MATH_EXACT)
+    u.set_schedule(kind=kind, math=native.MATH_EXACT, executor=executor)
     u.set_num_sets(sets)
     rng = np.random.default_rng(seed + sets)
     per_set = [[a * (1.0 + 0.05 * rng.standard_normal(a.shape)) for a in w.inputs] for _ in range(sets)]
@@ -86,12 +90,13 @@ def test_value_set_batches_match_oracle(name, size, seed, kind, sets):
         assert bits_equal(out[s], ref), f"set {s}"
 
 
-@pytest.mark.parametrize("kind", [native.SCHEDULE_PLAIN, native.SCHEDULE_LEVELS])
-def test_graph_replay_matches(kind):
+@pytest.mark.parametrize("kind", SCHEDULES)
+@pytest.mark.parametrize("executor", EXECUTORS)
+def test_graph_replay_matches(kind, executor):
     _, inp, gold = load_golden("cloth", 5)
     w = native.Workload("cloth", 5, 32)
     u = native.Unit.from_workload(w)
-    u.set_schedule(kind=kind, math=native.MATH_EXACT, use_graph=1)
+    u.set_schedule(kind=kind, math=native.MATH_EXACT, use_graph=1, executor=executor)
     for i, a in enumerate(split_inputs(w, inp)):
         u.set_arg(i, a)
     for _ in range(3):
@@ -110,7 +115,7 @@ def test_block_sizes_and_items_per_thread(tpb, items):
         for kind in SCHEDULES:
             for tile in (0, 3 * tpb):
                 u.set_schedule(kind=kind, math=native.MATH_EXACT, threads_per_block=tpb, items_per_tile=tile,
-                               items_per_thread=items)
+                               items_per_thread=items, executor=native.EXEC_INTERPRETER)
                 for i, a in enumerate(split_inputs(w, inp)):
                     u.set_arg(i, a)
                 u.run()
@@ -129,7 +134,7 @@ def test_lanes_per_item(lanes, tpb):
         for kind in SCHEDULES:
             for tile in (0, 3 * tpb // lanes + 1):
                 u.set_schedule(kind=kind, math=native.MATH_EXACT, threads_per_block=tpb, items_per_tile=tile,
-                               lanes_per_item=lanes)
+                               lanes_per_item=lanes, executor=native.EXEC_INTERPRETER)
                 u.set_num_sets(1)
                 for i, a in enumerate(split_inputs(w, inp)):
                     u.set_arg(i, a)
@@ -245,9 +250,50 @@ def test_larger_cases_match_oracle():
         ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
         assert rel_err(w.numeric, ref, floor_frac=1e-4) <= TOL
         u = native.Unit.from_workload(w)
-        for kind in SCHEDULES:
-            u.set_schedule(kind=kind, math=native.MATH_EXACT)
-            for i, a in enumerate(w.inputs):
-                u.set_arg(i, a)
+        for executor in EXECUTORS:
+            for kind in SCHEDULES:
+                u.set_schedule(kind=kind, math=native.MATH_EXACT, executor=executor)
+                for i, a in enumerate(w.inputs):
+                    u.set_arg(i, a)
+                u.run()
+                assert bits_equal(u.get_result(0), ref), (name, kind, executor)
+
+
+@pytest.mark.parametrize("tpb,items", [(32, 1), (96, 2), (128, 4), (256, 1), (512, 2)])
+@pytest.mark.parametrize("kind", SCHEDULES)
+def test_compiled_block_sizes(tpb, items, kind):
+    """The compiled executor at several block sizes and work items per thread
+    (partial last blocks, level dispatch boundaries) and 1 or 5 value sets:
+    bit-identical."""
+    for name, size, seed in [("cotan", 8, 22), ("cloth", 5, 32), ("neohookean", 1, 41)]:
+        _, inp, gold = load_golden(name, size)
+        w = native.Workload(name, size, seed)
+        u = native.Unit.from_workload(w)
+        u.set_schedule(kind=kind, math=native.MATH_EXACT, threads_per_block=tpb, items_per_thread=items)
+        for sets in (1, 5):
+            u.set_num_sets(sets)
+            for i, a in enumerate(split_inputs(w, inp)):
+                u.set_arg(i, np.tile(a, sets))
             u.run()
-            assert bits_equal(u.get_result(0), ref), (name, kind)
+            out = u.get_result(0).reshape(sets, -1)
+            assert bits_equal(out[0], gold) and bits_equal(out[-1], gold), (name, sets)
+
+
+def test_compiled_and_interpreted_per_kernel_shapes():
+    """Per-kernel block sizes (plain launches of the compiled executor) and
+    per-kernel timing work with both executors; values unchanged."""
+    _, inp, gold = load_golden("cloth", 5)
+    w = native.Workload("cloth", 5, 32)
+    u = native.Unit.from_workload(w)
+    for k in range(u.num_kernels):
+        u.set_kernel_shape(k, items=1 + (k % 2), lanes=1, tpb=32 * (1 + k % 4))
+    for executor in EXECUTORS:
+        u.set_schedule(kind=native.SCHEDULE_PLAIN, math=native.MATH_EXACT, executor=executor)
+        for i, a in enumerate(split_inputs(w, inp)):
+            u.set_arg(i, a)
+        u.run()
+        assert bits_equal(u.get_result(0), gold)
+        us = u.time_kernels(reps=2)
+        assert us.shape == (u.num_kernels,) and np.all(us >= 0)
+        u.run()
+        assert bits_equal(u.get_result(0), gold)
