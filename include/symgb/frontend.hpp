@@ -164,6 +164,7 @@ public:
     explicit PlanBuilder(const DeviceConfig& device) { plan_.device = device; }
     // Container of VAR(0..len-1, g) (an input) or of output expressions.
     void addContainer(const Symbolic* expr, std::size_t len);
+    // Builds the plan once; releases the output expressions it was given.
     Plan build();
 
 private:

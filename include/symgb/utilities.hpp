@@ -23,21 +23,41 @@ void collect(std::vector<std::pair<Symbolic*, std::size_t>>& out, C& c, Rest&...
 // assigned inside one BLOCK, and each entry becomes FIXED(variable, block).
 // The decomposition never splits a fixed block, so the block is evaluated as
 // one kernel instance (reference src/SymbolicUtilities.hpp:52-86).
-inline void makeFixedSpans(const std::vector<std::pair<Symbolic*, std::size_t>>& data) {
-    if (data.empty()) return;
+// The variables are numbered firstId, firstId + 1, ... in entry order;
+// returns how many were used.
+inline int makeFixedSpansAt(const std::vector<std::pair<Symbolic*, std::size_t>>& data, int firstId) {
+    if (data.empty()) return 0;
     std::unordered_map<hash_t, Symbolic, IdentityHash> exprMap;
     std::vector<Symbolic> assignments;
+    int next = firstId;
     for (auto& d : data)
         for (std::size_t i = 0; i < d.second; ++i) {
             Symbolic& var = exprMap[d.first[i].ahash()];
             if (var.op() == NOOP) {
-                var = Symbolic::generateUniqueVariable();
+                var = Symbolic(next++, EXPLICIT_INTERMEDIATE);
                 assignments.emplace_back(ASSIGN, var, d.first[i]);
             }
         }
     Symbolic block(BLOCK, assignments);
     for (auto& d : data)
         for (std::size_t i = 0; i < d.second; ++i) d.first[i] = Symbolic(FIXED, exprMap[d.first[i].ahash()], block);
+    return next - firstId;
+}
+
+// Number of variables makeFixedSpansAt would use (distinct algebraic hashes).
+inline int fixedVariableCount(const std::vector<std::pair<Symbolic*, std::size_t>>& data) {
+    std::unordered_map<hash_t, char, IdentityHash> seen;
+    for (auto& d : data)
+        for (std::size_t i = 0; i < d.second; ++i) seen.emplace(d.first[i].ahash(), 0);
+    return (int)seen.size();
+}
+
+// Numbers the variables from the process-wide unique-variable counter, as
+// Symbolic::generateUniqueVariable does.
+inline void makeFixedSpans(const std::vector<std::pair<Symbolic*, std::size_t>>& data) {
+    if (data.empty()) return;
+    int& counter = Symbolic::uniqueVariableCounter();
+    counter += makeFixedSpansAt(data, counter);
 }
 
 template <class... Conts>

@@ -213,12 +213,19 @@ Plan PlanBuilder::build() {
 
     // The blocks' expressions are released in parallel (most of their nodes
     // belong to one block; reference counts are atomic meanwhile).
+    // So are the output expressions this builder holds (the containers' whole
+    // expression graph, often hundreds of millions of nodes): build() consumes
+    // them.
     {
         Symbolic::ConcurrentRefs concurrent;
         parallelFor(blocks.size(), 1024, [&](std::size_t b, std::size_t e) {
             for (std::size_t i = b; i < e; ++i) blocks[i] = ExpressionBlock();
         });
+        parallelFor(outputExpressions_.size(), 1024, [&](std::size_t b, std::size_t e) {
+            for (std::size_t i = b; i < e; ++i) outputExpressions_[i] = Symbolic();
+        });
     }
+    outputExpressions_.clear();
     return std::move(plan_);
 }
 

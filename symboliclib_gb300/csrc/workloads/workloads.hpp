@@ -16,6 +16,7 @@
 #include <functional>
 #include <map>
 #include <tuple>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -69,31 +70,73 @@ struct CSC {
     std::size_t nnz() const { return values.size(); }
 };
 
-// Duplicates are summed as ((t1 + t2) + t3) ... in triplet order.
-template <class NT>
-CSC<NT> assemble(int rows, int cols, const std::vector<Triplet<NT>>& trips) {
-    std::vector<std::map<int, NT>> colsMap(cols);
-    for (const auto& t : trips) {
-        auto& m = colsMap[t.col];
-        auto it = m.find(t.row);
-        if (it == m.end())
-            m.emplace(t.row, t.value);
-        else
-            it->second = it->second + t.value;
+// Runs fn(begin, end) over [0, n): serially (the default of the model
+// functions below) or, when the engine's front end passes its worker pool,
+// in parallel chunks.  Model code only parallelises loops whose iterations
+// write disjoint results, so the expressions built do not depend on it.
+struct SerialFor {
+    template <class F>
+    void operator()(std::size_t n, F&& fn) const {
+        fn(std::size_t(0), n);
     }
+};
+
+// Duplicates are summed as ((t1 + t2) + t3) ... in triplet order.  Columns are
+// independent: triplets are bucketed by column (keeping their order) and the
+// columns summed by `forEach`.
+template <class NT, class For = SerialFor>
+CSC<NT> assemble(int rows, int cols, const std::vector<Triplet<NT>>& trips, For&& forEach = For()) {
+    std::vector<std::size_t> start((std::size_t)cols + 1, 0), order(trips.size());
+    for (const auto& t : trips) ++start[(std::size_t)t.col + 1];
+    for (int c = 0; c < cols; ++c) start[c + 1] += start[c];
+    {
+        std::vector<std::size_t> fill(start.begin(), start.end() - 1);
+        for (std::size_t i = 0; i < trips.size(); ++i) order[fill[trips[i].col]++] = i;
+    }
+    std::vector<std::vector<std::pair<int, NT>>> colEntries(cols);
+    forEach((std::size_t)cols, [&](std::size_t cb, std::size_t ce) {
+        for (std::size_t c = cb; c < ce; ++c) {
+            std::map<int, NT> m;
+            for (std::size_t q = start[c]; q < start[c + 1]; ++q) {
+                const auto& t = trips[order[q]];
+                auto it = m.find(t.row);
+                if (it == m.end())
+                    m.emplace(t.row, t.value);
+                else
+                    it->second = it->second + t.value;
+            }
+            colEntries[c].assign(m.begin(), m.end());
+        }
+    });
     CSC<NT> A;
     A.rows = rows;
     A.cols = cols;
     A.colPtr.assign(cols + 1, 0);
-    for (int c = 0; c < cols; ++c) {
-        A.colPtr[c + 1] = A.colPtr[c] + (int)colsMap[c].size();
-        for (auto& e : colsMap[c]) {
-            A.rowIdx.push_back(e.first);
-            A.values.push_back(e.second);
+    for (int c = 0; c < cols; ++c) A.colPtr[c + 1] = A.colPtr[c] + (int)colEntries[c].size();
+    A.rowIdx.resize(A.colPtr[cols]);
+    A.values.resize(A.colPtr[cols]);
+    forEach((std::size_t)cols, [&](std::size_t cb, std::size_t ce) {
+        for (std::size_t c = cb; c < ce; ++c) {
+            int k = A.colPtr[c];
+            for (auto& e : colEntries[c]) {
+                A.rowIdx[k] = e.first;
+                A.values[k++] = std::move(e.second);
+            }
+            colEntries[c] = {};
         }
-    }
+    });
     return A;
 }
+
+// A `fix` with a member batch(K9s, D9s, forEach) treats all faces at once
+// (with the same result as fix(K9s[f], D9s[f]) face after face).
+template <class F, class A, class For, class = void>
+struct HasBatchFix : std::false_type {};
+template <class F, class A, class For>
+struct HasBatchFix<F, A, For,
+                   std::void_t<decltype(std::declval<const F&>().batch(std::declval<std::vector<A>&>(),
+                                                                       std::declval<std::vector<A>&>(),
+                                                                       std::declval<For&>()))>> : std::true_type {};
 
 // Lower triangle (row >= col) of a CSC matrix.
 template <class NT>
@@ -430,14 +473,20 @@ inline void clothState(const ClothRest& r, std::uint64_t seed, std::vector<doubl
 // implementation/stretch_shear_forces_impl.hpp:63-261,
 // implementation/bend_quadratic_forces.cpp:53-155).  `fix(K9, D9)` is applied
 // to every face's 9x9 stiffness and damping blocks (makeFixed for symbolic
-// scalars, nothing for double).
-template <class NT, class Fix>
-CSC<NT> clothMatrix(const ClothRest& r, const std::vector<NT>& X, const std::vector<NT>& Vel, Fix&& fix) {
+// scalars, nothing for double).  The faces' blocks are independent and built
+// by `forEach` (serially by default); `fix` and the assembly then proceed in
+// face order, so the result does not depend on it.
+template <class NT, class Fix, class For = SerialFor>
+CSC<NT> clothMatrix(const ClothRest& r, const std::vector<NT>& X, const std::vector<NT>& Vel, Fix&& fix,
+                    For&& forEach = For()) {
     using std::sqrt;
     const int n = r.mesh.nv;
     const auto& p = r.p;
     std::vector<Triplet<NT>> tK, tD;
-    for (std::size_t fi = 0; fi < r.mesh.F.size(); ++fi) {
+    const std::size_t nf = r.mesh.F.size();
+    std::vector<std::array<NT, 81>> K9s(nf), D9s(nf);
+    forEach(nf, [&](std::size_t fb, std::size_t fe) {
+    for (std::size_t fi = fb; fi < fe; ++fi) {
         const auto& f = r.mesh.F[fi];
         const double a = r.area[fi];
         const auto& Vi = r.Vinv[fi];
@@ -459,7 +508,8 @@ CSC<NT> clothMatrix(const ClothRest& r, const std::vector<NT>& X, const std::vec
         for (int i = 0; i < 3; ++i)
             for (int d = 0; d < 3; ++d) v[i][d] = Vel[f[i] + d * n];
 
-        std::array<NT, 81> K9, D9;
+        std::array<NT, 81>& K9 = K9s[fi];
+        std::array<NT, 81>& D9 = D9s[fi];
         // stretch
         NT C[2] = {NT(a) * (Jnorm[0] - NT(1.0)), NT(a) * (Jnorm[1] - NT(1.0))};
         NT dC[3][3][2];  // dC[i][d][c]
@@ -505,7 +555,19 @@ CSC<NT> clothMatrix(const ClothRest& r, const std::vector<NT>& X, const std::vec
                         D9[(3 * i + d) * 9 + 3 * j + e] = Ds + Dh;
                     }
             }
-        fix(K9, D9);
+    }
+    });
+    using FixT = std::decay_t<Fix>;
+    using ForT = std::decay_t<For>;
+    if constexpr (HasBatchFix<FixT, std::array<NT, 81>, ForT>::value) {
+        fix.batch(K9s, D9s, forEach);
+    } else {
+        for (std::size_t fi = 0; fi < nf; ++fi) fix(K9s[fi], D9s[fi]);
+    }
+    for (std::size_t fi = 0; fi < nf; ++fi) {
+        const auto& f = r.mesh.F[fi];
+        const std::array<NT, 81>& K9 = K9s[fi];
+        const std::array<NT, 81>& D9 = D9s[fi];
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j)
                 for (int d = 0; d < 3; ++d)
@@ -517,6 +579,14 @@ CSC<NT> clothMatrix(const ClothRest& r, const std::vector<NT>& X, const std::vec
                         }
                     }
     }
+    forEach(nf, [&](std::size_t fb, std::size_t fe) {
+        for (std::size_t fi = fb; fi < fe; ++fi) {
+            K9s[fi] = {};
+            D9s[fi] = {};
+        }
+    });
+    K9s.clear();
+    D9s.clear();
     // quadratic bend: constant stiffness k Q and damping kd Q per interior edge
     std::vector<Triplet<NT>> bK, bD;
     for (std::size_t e = 0; e < r.E4.size(); ++e)
@@ -533,29 +603,31 @@ CSC<NT> clothMatrix(const ClothRest& r, const std::vector<NT>& X, const std::vec
                     }
                 }
     const int N = 3 * n;
-    CSC<NT> Kss = assemble(N, N, tK), Dss = assemble(N, N, tD), Kb = assemble(N, N, bK), Db = assemble(N, N, bD);
+    CSC<NT> Kss = assemble(N, N, tK, forEach), Dss = assemble(N, N, tD, forEach), Kb = assemble(N, N, bK, forEach),
+            Db = assemble(N, N, bD, forEach);
+    tK.clear();
+    tD.clear();
     // A = M - h (D + h K) on the union pattern, lower triangle.
     const double mass = p.totalMass / n;
     std::vector<std::map<int, NT>> Kc(N), Dc(N);
-    auto addInto = [](std::vector<std::map<int, NT>>& dst, const CSC<NT>& S) {
-        for (int c = 0; c < S.cols; ++c)
-            for (int k = S.colPtr[c]; k < S.colPtr[c + 1]; ++k) {
-                auto it = dst[c].find(S.rowIdx[k]);
-                if (it == dst[c].end())
-                    dst[c].emplace(S.rowIdx[k], S.values[k]);
-                else
-                    it->second = it->second + S.values[k];
-            }
+    auto addInto = [](std::vector<std::map<int, NT>>& dst, const CSC<NT>& S, std::size_t c) {
+        for (int k = S.colPtr[c]; k < S.colPtr[c + 1]; ++k) {
+            auto it = dst[c].find(S.rowIdx[k]);
+            if (it == dst[c].end())
+                dst[c].emplace(S.rowIdx[k], S.values[k]);
+            else
+                it->second = it->second + S.values[k];
+        }
     };
-    addInto(Kc, Kss);
-    addInto(Kc, Kb);
-    addInto(Dc, Dss);
-    addInto(Dc, Db);
-    CSC<NT> A;
-    A.rows = N;
-    A.cols = N;
-    A.colPtr.assign(N + 1, 0);
-    for (int c = 0; c < N; ++c) {
+    // Column by column (columns are independent).
+    std::vector<std::vector<std::pair<int, NT>>> colA(N);
+    forEach((std::size_t)N, [&](std::size_t cb, std::size_t ce) {
+    for (std::size_t cc = cb; cc < ce; ++cc) {
+        const int c = (int)cc;
+        addInto(Kc, Kss, cc);
+        addInto(Kc, Kb, cc);
+        addInto(Dc, Dss, cc);
+        addInto(Dc, Db, cc);
         std::map<int, int> rowsU;
         for (auto& e : Kc[c]) rowsU[e.first] |= 1;
         for (auto& e : Dc[c]) rowsU[e.first] |= 2;
@@ -577,11 +649,33 @@ CSC<NT> clothMatrix(const ClothRest& r, const std::vector<NT>& X, const std::vec
             } else {
                 val = NT(mass);
             }
-            A.rowIdx.push_back(row);
-            A.values.push_back(val);
+            colA[c].emplace_back(row, std::move(val));
         }
-        A.colPtr[c + 1] = (int)A.values.size();
+        Kc[c].clear();
+        Dc[c].clear();
     }
+    });
+    CSC<NT> A;
+    A.rows = N;
+    A.cols = N;
+    A.colPtr.assign(N + 1, 0);
+    for (int c = 0; c < N; ++c) A.colPtr[c + 1] = A.colPtr[c] + (int)colA[c].size();
+    A.rowIdx.resize(A.colPtr[N]);
+    A.values.resize(A.colPtr[N]);
+    forEach((std::size_t)N, [&](std::size_t cb, std::size_t ce) {
+        for (std::size_t c = cb; c < ce; ++c) {
+            int k = A.colPtr[c];
+            for (auto& e : colA[c]) {
+                A.rowIdx[k] = e.first;
+                A.values[k++] = std::move(e.second);
+            }
+            colA[c] = {};
+        }
+    });
+    for (CSC<NT>* M : {&Kss, &Dss, &Kb, &Db})  // the summands' handles, dropped in parallel too
+        forEach(M->values.size(), [&](std::size_t b, std::size_t e) {
+            for (std::size_t i = b; i < e; ++i) M->values[i] = NT();
+        });
     return A;
 }
 

@@ -10,6 +10,7 @@
 
 #include "symgb/differentiation.hpp"
 #include "symgb/frontend.hpp"
+#include "symgb/parallel.hpp"
 #include "symgb/plan_image.hpp"
 #include "symgb/utilities.hpp"
 #include "workloads.hpp"
@@ -25,6 +26,7 @@ struct Workload {
     std::vector<double> numeric;  // model evaluated in double
     std::string planText;
     double frontSeconds = 0.0;
+    double modelSeconds = 0.0;  // building the symbolic outputs (the workload's own model code)
     std::uint64_t outputs = 0;
     int rows = 0, cols = 0;              // output matrix (CSC workloads)
     std::vector<int> colPtr, rowIdx;
@@ -43,6 +45,38 @@ struct Fix {
     template <class A>
     void operator()(A& K9, A& D9) const {
         symgb::makeFixed(K9, D9);
+    }
+    // All faces at once: each face's variable count first, then every face
+    // numbered from its prefix sum, so the variables are those of the
+    // face-by-face loop.
+    template <class A, class For>
+    void batch(std::vector<A>& K9s, std::vector<A>& D9s, For& forEach) const {
+        const std::size_t n = K9s.size();
+        auto spans = [&](std::size_t f) {
+            return std::vector<std::pair<symgb::Symbolic*, std::size_t>>{{K9s[f].data(), K9s[f].size()},
+                                                                         {D9s[f].data(), D9s[f].size()}};
+        };
+        std::vector<int> first(n + 1, 0);
+        forEach(n, [&](std::size_t b, std::size_t e) {
+            for (std::size_t f = b; f < e; ++f) first[f + 1] = symgb::fixedVariableCount(spans(f));
+        });
+        int& counter = symgb::Symbolic::uniqueVariableCounter();
+        first[0] = counter;
+        for (std::size_t f = 0; f < n; ++f) first[f + 1] += first[f];
+        forEach(n, [&](std::size_t b, std::size_t e) {
+            for (std::size_t f = b; f < e; ++f) symgb::makeFixedSpansAt(spans(f), first[f]);
+        });
+        counter = first[n];
+    }
+};
+// The front end's worker pool for the independent per-element parts of the
+// model code; handles to shared nodes (the input variables) are copied from
+// several threads, so reference counts are atomic meanwhile.
+struct PoolFor {
+    template <class F>
+    void operator()(std::size_t n, F&& fn) const {
+        symgb::Symbolic::ConcurrentRefs concurrent;
+        symgb::parallelFor(n, 64, [&](std::size_t b, std::size_t e) { fn(b, e); });
     }
 };
 struct NoFix {
@@ -96,7 +130,7 @@ int symgbw_build(const char* name, int size, unsigned long long seed, int vector
             std::vector<double> X, vel;
             clothState(r, seed, X, vel);
             auto XS = variables(X.size(), 0), VS = variables(vel.size(), 1);
-            CSC<symgb::Symbolic> A = clothMatrix(r, XS, VS, Fix());
+            CSC<symgb::Symbolic> A = clothMatrix(r, XS, VS, Fix(), PoolFor());
             pb.addContainer(XS.data(), XS.size());
             pb.addContainer(VS.data(), VS.size());
             pb.addContainer(A.values.data(), A.values.size());
@@ -146,6 +180,7 @@ int symgbw_build(const char* name, int size, unsigned long long seed, int vector
             g_err = "unknown workload " + n;
             return -1;
         }
+        w->modelSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         w->plan = pb.build();
         w->frontSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         symgb::buildPlanImage(w->plan, w->image, 128);
@@ -186,6 +221,7 @@ uint64_t symgbw_plan_text(symgbw_t w, char* buf, uint64_t cap) {
     return w->planText.size();
 }
 double symgbw_front_seconds(symgbw_t w) { return w->frontSeconds; }
+double symgbw_model_seconds(symgbw_t w) { return w->modelSeconds; }
 
 // Pattern of the output matrix (CSC; 0 rows when the workload has none):
 // col_ptr has cols + 1 entries, row_idx nnz.

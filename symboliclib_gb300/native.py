@@ -162,6 +162,8 @@ def workloads() -> C.CDLL:
         lib.symgbw_plan_text.argtypes = [C.c_void_p, C.c_char_p, C.c_uint64]
         lib.symgbw_front_seconds.restype = C.c_double
         lib.symgbw_front_seconds.argtypes = [C.c_void_p]
+        lib.symgbw_model_seconds.restype = C.c_double
+        lib.symgbw_model_seconds.argtypes = [C.c_void_p]
         lib.symgbw_pattern.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                        C.POINTER(C.POINTER(C.c_int)), C.POINTER(C.POINTER(C.c_int))]
         lib._typed = True
@@ -204,7 +206,8 @@ class Workload:
         n = C.c_uint64()
         p = lib.symgbw_numeric(h, C.byref(n))
         self.numeric = _array(p, n.value, np.float64)
-        self.front_seconds = lib.symgbw_front_seconds(h)
+        self.front_seconds = lib.symgbw_front_seconds(h)  # model construction + planning
+        self.model_seconds = lib.symgbw_model_seconds(h)  # model construction alone
 
     def pattern(self):
         """(rows, cols, col_ptr, row_idx) of the output matrix in CSC form."""

@@ -1,5 +1,7 @@
-"""The front end's parallel passes (lockstep walk over kernel instances, block
-extraction) give the same plan as running them on one thread."""
+"""The front end's parallel passes (the cloth model's per-face blocks,
+makeFixed numbering and column assembly; lockstep walk over kernel
+instances; block extraction; release of the expression graph) give the same
+plan as running them on one thread."""
 import os
 import subprocess
 import sys
