@@ -1,12 +1,15 @@
 """Schedule autotuner and learned schedule proposer.
 
-The schedule of a unit (launch structure, fusion depth, block size, work items
-per thread, tile size) changes only speed, never values.  `exhaustive` times
-every schedule in `SPACE` on the GPU and returns the fastest.  `CostModel` is
-an MLP (the engine's FP32 kernels, native.MLP) that predicts the log run time
-of a unit under a schedule from plan features; `propose` ranks all schedules
-by predicted time and times only the top k, so tuning costs k timings instead
-of len(SPACE).  The training data are timings the tuner itself collected."""
+The schedule of a unit (executor, launch structure, fusion depth, block size,
+work items per thread, tile size) changes only speed, never values.
+`exhaustive` times every schedule in `SPACE` on the GPU and returns the
+fastest; a compiled-executor schedule is compiled (NVRTC) the first time it
+is timed, and that compile time counts as tuning time.  `CostModel` is an MLP
+(the engine's FP32 kernels, native.MLP) that predicts the log run time of a
+unit under a schedule from plan features; `tune_with_model` times the
+default schedule and the model's k - 1 best-ranked others, so tuning costs k
+timings (and at most k compiles) instead of len(SPACE).  The training data
+are timings the tuner itself collected."""
 from __future__ import annotations
 
 import ctypes as C
@@ -23,26 +26,36 @@ KINDS = {"plain": (native.SCHEDULE_PLAIN, 0), "levels": (native.SCHEDULE_LEVELS,
          "fused2": (native.SCHEDULE_LEVELS, 2), "persistent": (native.SCHEDULE_PERSISTENT, 0)}
 
 
+EXECUTORS = {"compiled": native.EXEC_COMPILED, "interpreter": native.EXEC_INTERPRETER}
+
+
 @dataclass(frozen=True)
 class Sched:
     kind: str
     items: int
     tpb: int
-    tile: int  # a tile is (tpb / lanes) * items * tile work items
-    lanes: int = 1
+    tile: int  # interpreter: a tile is (tpb / lanes) * items * tile work items
+    lanes: int = 1  # interpreter only
+    executor: str = "interpreter"
 
     def apply(self, unit: native.Unit, math_mode: int = native.MATH_FAST, graph: int = 1) -> None:
         k, depth = KINDS[self.kind]
         unit.set_schedule(kind=k, math=math_mode, threads_per_block=self.tpb,
                           items_per_tile=self.tpb // self.lanes * self.items * self.tile, items_per_thread=self.items,
-                          use_graph=graph, fusion_depth=depth, lanes_per_item=self.lanes)
+                          use_graph=graph, fusion_depth=depth, lanes_per_item=self.lanes,
+                          executor=EXECUTORS[self.executor])
 
 
 # (items per thread, lanes per item): several items per thread for small
 # register files, several lanes per item for large ones
 SHAPES = ((1, 1), (2, 1), (4, 1), (1, 2), (1, 4))
-SPACE = [Sched(k, i, t, f, l) for k, (i, l), t, f in itertools.product(KINDS, SHAPES, (64, 128, 256), (1, 4))]
-DEFAULT = Sched("levels", 1, 128, 1)
+INTERPRETER_SPACE = [Sched(k, i, t, f, l) for k, (i, l), t, f in
+                     itertools.product(KINDS, SHAPES, (64, 128, 256), (1, 4))]
+# The compiled executor has no tiles, lanes or fusion depth: kind x items x tpb.
+COMPILED_SPACE = [Sched(k, i, t, 1, 1, "compiled") for k, i, t in
+                  itertools.product(("plain", "levels", "persistent"), (1, 2, 4), (64, 128, 256))]
+SPACE = COMPILED_SPACE + INTERPRETER_SPACE
+DEFAULT = Sched("levels", 1, 128, 1, 1, "compiled")
 
 
 def time_schedule(unit: native.Unit, sched: Sched, stream, flush=None, runs: int = 5, warmup: int = 2) -> float:
@@ -111,7 +124,7 @@ def plan_features(stats: native.Stats, num_sets: int) -> np.ndarray:
 
 
 def schedule_features(s: Sched) -> np.ndarray:
-    onehot = [1.0 if s.kind == k else 0.0 for k in KINDS]
+    onehot = [1.0 if s.kind == k else 0.0 for k in KINDS] + [1.0 if s.executor == "compiled" else 0.0]
     return np.array(onehot + [math.log2(s.lanes), math.log2(s.items), math.log2(s.tpb), math.log2(s.tile)], np.float32)
 
 
@@ -121,7 +134,9 @@ def features(stats: native.Stats, num_sets: int, s: Sched) -> np.ndarray:
     # interactions: work per launch under this schedule
     # register file bytes per thread under this shape (occupancy)
     regfile = np.array([math.log2(1.0 + float(stats.max_registers) * s.items / s.lanes)], np.float32)
-    return np.concatenate([p, q, p[:6] * q[-3] / 8.0, p[:6] * q[-2] / 8.0, p[:6] * q[-4] / 8.0, regfile])
+    compiled = 1.0 if s.executor == "compiled" else 0.0
+    return np.concatenate([p, q, p[:6] * q[-3] / 8.0, p[:6] * q[-2] / 8.0, p[:6] * q[-4] / 8.0, regfile,
+                           p[:6] * compiled, regfile * (1.0 - compiled)])
 
 
 class CostModel:
@@ -143,10 +158,19 @@ class CostModel:
         return np.exp(self.net.predict((X - self.mu) / self.sd))
 
 
-def propose(model: CostModel, stats: native.Stats, num_sets: int, k: int = 3, space=SPACE) -> list[Sched]:
+def propose(model: CostModel, stats: native.Stats, num_sets: int, k: int = 3, space=SPACE,
+            keep=DEFAULT) -> list[Sched]:
+    """k schedules to time: `keep` (the default schedule; None for none) and
+    the model's best-ranked others."""
     X = np.stack([features(stats, num_sets, s) for s in space])
     order = np.argsort(model.predict_us(X))
-    return [space[i] for i in order[:k]]
+    picks = [keep] if keep is not None else []
+    for i in order:
+        if len(picks) >= k:
+            break
+        if space[i] != keep:
+            picks.append(space[i])
+    return picks
 
 
 def tune_with_model(unit: native.Unit, model: CostModel, stream, flush=None, k: int = 3, runs: int = 5) -> TuneResult:
@@ -166,6 +190,7 @@ def tune_with_model(unit: native.Unit, model: CostModel, stream, flush=None, k: 
 # Launch shapes a single kernel can take: (items per thread, lanes per item)
 # x threads per block.
 KERNEL_SHAPES = [(i, l, t) for (i, l) in SHAPES for t in (64, 128, 256)]
+COMPILED_KERNEL_SHAPES = [(i, 1, t) for i in (1, 2, 4) for t in (64, 128, 256)]
 
 _OPNAMES = {5: "add", 6: "sub", 7: "mul", 8: "div", 9: "neg", 10: "sqrt", 11: "rec", 12: "fma", 23: "fma", 24: "fma",
             25: "fma", 26: "div", 27: "sqrt", 28: "rec"}
@@ -228,20 +253,24 @@ class PerKernel:
     """A schedule kind run with the kernels' own launch shapes: tiles follow
     each kernel's shape (no fixed tile size)."""
     kind: str = "plain"
+    executor: str = "interpreter"
 
     def apply(self, unit: native.Unit, math_mode: int = native.MATH_FAST, graph: int = 1) -> None:
         k, depth = KINDS[self.kind]
-        unit.set_schedule(kind=k, math=math_mode, items_per_tile=0, use_graph=graph, fusion_depth=depth)
+        unit.set_schedule(kind=k, math=math_mode, items_per_tile=0, use_graph=graph, fusion_depth=depth,
+                          executor=EXECUTORS[self.executor])
 
     def __str__(self) -> str:
-        return f"{self.kind} with per-kernel shapes"
+        return f"{self.kind} with per-kernel shapes ({self.executor})"
 
 
-def tune_kernels(unit: native.Unit, flush=None, shapes=None, reps: int = 5) -> KernelTuneResult:
+def tune_kernels(unit: native.Unit, flush=None, shapes=None, reps: int = 5,
+                 executor: str = "interpreter") -> KernelTuneResult:
     """Exhaustive per-kernel tuning: every kernel timed in every shape."""
-    shapes = KERNEL_SHAPES if shapes is None else shapes
+    if shapes is None:
+        shapes = KERNEL_SHAPES if executor == "interpreter" else COMPILED_KERNEL_SHAPES
     t0 = time.perf_counter()
-    PerKernel("plain").apply(unit)
+    PerKernel("plain", executor).apply(unit)
     nk = unit.num_kernels
     table = {}
     for sh in shapes:

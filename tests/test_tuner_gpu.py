@@ -34,13 +34,15 @@ def test_fusion_depth_and_graphs_bit_exact(depth, graph):
         _, inp, gold = load_golden(name, size)
         w = native.Workload(name, size, seed)
         u = native.Unit.from_workload(w)
-        u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_EXACT, fusion_depth=depth, use_graph=graph)
+        u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_EXACT, fusion_depth=depth, use_graph=graph,
+                       executor=native.EXEC_INTERPRETER)
         for i, a in enumerate(split_inputs(w, inp)):
             u.set_arg(i, a)
         for _ in range(2):
             u.run()
             assert bits_equal(u.get_result(0), gold), (name, depth, graph)
-        u.set_schedule(kind=native.SCHEDULE_PERSISTENT, math=native.MATH_EXACT, use_graph=graph)
+        u.set_schedule(kind=native.SCHEDULE_PERSISTENT, math=native.MATH_EXACT, use_graph=graph,
+                       executor=native.EXEC_INTERPRETER)
         u.run()
         assert bits_equal(u.get_result(0), gold), (name, "persistent", graph)
 
@@ -114,46 +116,56 @@ def test_mlp_training_fits_a_smooth_function():
     assert after < 0.05 * before and after < 0.01
 
 
-def test_learned_proposer_beats_untrained_choice():
-    """What the trained network gains.  The cost model is trained on the
-    tuner's timings of one set of units and evaluated on held-out units.
-    Timing only its top-K schedules costs K timings instead of len(SPACE)
-    (at least 10x fewer) and must stay within 10% mean regret of exhaustive
-    search, and do better than the same budget spent without the network (K
-    schedules drawn at random)."""
+def test_learned_proposer_gain():
+    """What the trained network gains, measured honestly.  The cost model is
+    trained on the tuner's own exhaustive timings of one set of units and
+    evaluated on held-out units (cotangent Laplacians and cloth Hessians of
+    other sizes, one and eight value sets, random expression plans).  With the
+    network, tuning times the default schedule plus the model's K - 1
+    best-ranked others; without it, the default plus K - 1 others drawn at
+    random.  K is at least 10x smaller than the schedule space.  Mean regret
+    against exhaustive search must be at most 5% and no worse than without
+    the network."""
     K = len(tuner.SPACE) // 15
-    train_units = [("random", 60000, s) for s in range(10)] + [("cotan", 100, 1), ("cloth", 20, 2), ("ata", 60, 3)]
-    test_units = [("random", 90000, 100 + s) for s in range(6)] + [("cotan", 150, 7), ("cloth", 26, 8),
-                                                                    ("neohookean", 3, 9)]
+    train_units = [("random", 60000, s, 1) for s in range(6)] + [("cotan", 100, 1, 1), ("cloth", 20, 2, 1),
+                                                                  ("cloth", 12, 3, 8), ("ata", 60, 3, 1)]
+    test_units = [("random", 90000, 100 + s, 1) for s in range(2)] + [("cotan", 150, 7, 1), ("cotan", 220, 8, 1),
+                                                                     ("cloth", 26, 8, 1), ("cloth", 16, 9, 8)]
     X, y, held = [], [], []
     for spec in train_units + test_units:
-        w = native.Workload(*spec)
+        name, size, seed, S = spec
+        w = native.Workload(name, size, seed)
         u = native.Unit.from_workload(w)
+        u.set_num_sets(S)
         for i, a in enumerate(w.inputs):
-            u.set_arg(i, a)
+            u.set_arg(i, np.tile(a, S))
         stream = tuner.bind_stream(u)
         res = tuner.exhaustive(u, stream, runs=5)
         st = u.stats()
         if spec in train_units:
-            for s, t in res.timings.items():
-                X.append(tuner.features(st, 1, s))
+            for sch, t in res.timings.items():
+                X.append(tuner.features(st, S, sch))
                 y.append(t)
         else:
-            held.append((res, st))
+            held.append((res, st, S))
     model = tuner.CostModel(seed=0)
     model.fit(np.stack(X), np.array(y), epochs=3000)
     rng = np.random.default_rng(4)
-    regret_model, regret_random = [], []
-    for res, st in held:
-        picks = tuner.propose(model, st, 1, k=K)
-        regret_model.append(min(res.timings[s] for s in picks if s in res.timings) / res.best_us - 1.0)
-        for _ in range(20):  # expected regret of K random picks
-            blind = [tuner.SPACE[i] for i in rng.choice(len(tuner.SPACE), K, replace=False)]
-            regret_random.append(min(res.timings[s] for s in blind if s in res.timings) / res.best_us - 1.0)
-    print(f"mean regret: model top-{K}", np.mean(regret_model), f"random {K}", np.mean(regret_random))
+    regret_model, regret_blind, regret_default = [], [], []
+    others = [sch for sch in tuner.SPACE if sch != tuner.DEFAULT]
+    for res, st, S in held:
+        picks = tuner.propose(model, st, S, k=K)
+        assert len(picks) == K and picks[0] == tuner.DEFAULT
+        regret_model.append(min(res.timings[sch] for sch in picks if sch in res.timings) / res.best_us - 1.0)
+        regret_default.append(res.timings[tuner.DEFAULT] / res.best_us - 1.0)
+        for _ in range(50):  # expected regret of the default plus K - 1 random picks
+            blind = [tuner.DEFAULT] + [others[i] for i in rng.choice(len(others), K - 1, replace=False)]
+            regret_blind.append(min(res.timings[sch] for sch in blind if sch in res.timings) / res.best_us - 1.0)
+    print(f"mean regret: default {np.mean(regret_default):.4f}, default + {K - 1} random "
+          f"{np.mean(regret_blind):.4f}, default + model's top {K - 1} {np.mean(regret_model):.4f}")
     assert len(tuner.SPACE) / K >= 10
-    assert np.mean(regret_model) <= 0.10
-    assert np.mean(regret_model) < np.mean(regret_random)
+    assert np.mean(regret_model) <= 0.05
+    assert np.mean(regret_model) <= np.mean(regret_blind)
 
 
 def test_per_kernel_shapes_are_exact_and_timed():
@@ -172,9 +184,10 @@ def test_per_kernel_shapes_are_exact_and_timed():
                 i, l, t = tuner.KERNEL_SHAPES[rng.integers(len(tuner.KERNEL_SHAPES))]
                 u.set_kernel_shape(k, i, l, t)
             for kind in (native.SCHEDULE_PLAIN, native.SCHEDULE_LEVELS):
-                u.set_schedule(kind=kind, math=native.MATH_EXACT)
-                u.run()
-                assert bits_equal(u.get_result(0), gold), (name, trial, kind)
+                for executor in (native.EXEC_COMPILED, native.EXEC_INTERPRETER):
+                    u.set_schedule(kind=kind, math=native.MATH_EXACT, executor=executor)
+                    u.run()
+                    assert bits_equal(u.get_result(0), gold), (name, trial, kind, executor)
         flush = torch.empty(1 << 20, dtype=torch.float32, device="cuda")
         t = u.time_kernels(3, flush)
         assert len(t) == u.num_kernels
