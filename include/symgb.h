@@ -339,9 +339,13 @@ int symgb_measure_fp64_rate(double* flops_per_second);
  * one static device array of SYMGB_STATIC_SCRATCH_BYTES that every GPU loading
  * this entry point keeps until exit; plans that need more are rejected with
  * SYMGB_ERR_ARGUMENT.  No cudaMalloc / cudaFree or other allocating call is
- * made.  The first call on a device looks up the array's device address, so
- * make it before any stream capture.  Calls share the array and return when the
- * work on `stream` is done; calls from several threads must not overlap. */
+ * made on the device side; on the host each call still builds the plan's
+ * tables, programs and tiles in temporary host buffers and copies them into
+ * the array, so its host cost grows with the plan.  The first call on a device
+ * looks up the array's device address.  Every call reads a status word back
+ * on `stream` and waits for `stream` before it returns, so a call cannot be
+ * recorded into a CUDA graph.  Calls share the array; calls from several
+ * threads must not overlap. */
 #define SYMGB_STATIC_SCRATCH_BYTES (32ull << 20)
 int symgb_run_static(symgb_unit_t u, const uint32_t* index_data, const uint32_t* out_index_data,
                      const double* const_data, const double* const* inputs, double* const* outputs, void* stream);

@@ -230,9 +230,11 @@ extern "C" int symgb_run_static(symgb_unit_t u, const uint32_t* index_data, cons
             gatherKernel<<<(unsigned)((len + 255) / 256), 256, 0, stream>>>(x, ids + u->outStart[k], len, 1u, outputs[k]);
     }
     STATIC_CUDA(cudaGetLastError());
-    STATIC_CUDA(cudaStreamSynchronize(stream));
+    // The status word is read back on the caller's stream, so the call waits
+    // for its own work only, not for other streams of the device.
     int err = 0;
-    STATIC_CUDA(cudaMemcpy(&err, base + oBar + sizeof(BarrierState), sizeof(int), cudaMemcpyDeviceToHost));
+    STATIC_CUDA(cudaMemcpyAsync(&err, base + oBar + sizeof(BarrierState), sizeof(int), cudaMemcpyDeviceToHost, stream));
+    STATIC_CUDA(cudaStreamSynchronize(stream));
     if (err) return failStatic(err, "device-side wait timed out (grid barrier)");
     return SYMGB_OK;
 }

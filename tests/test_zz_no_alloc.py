@@ -76,6 +76,26 @@ def test_static_entry_matches_normal_entry(name, size, seed):
         lib.symgb_unit_destroy(h)
 
 
+def test_static_entry_allocates_no_device_memory():
+    """Once the first call has loaded the module (and with it the static
+    array), further calls leave the device's free memory unchanged."""
+    import torch
+    w = native.Workload("cloth", 8, 4)
+    lib, h = static_unit(w)
+    try:
+        inputs_dev = [torch.from_numpy(a).cuda() for a in w.inputs]
+        outputs_dev = [torch.empty(len(w.numeric), dtype=torch.float64, device="cuda")]
+        native.check(run_static(lib, h, w, inputs_dev, outputs_dev))
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
+        for _ in range(3):
+            native.check(run_static(lib, h, w, inputs_dev, outputs_dev))
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] >= free_before
+    finally:
+        lib.symgb_unit_destroy(h)
+
+
 def test_static_entry_rejects_plans_beyond_its_scratch():
     import torch
     w = native.Workload("cotan", 8, 1)
