@@ -43,10 +43,11 @@ FALLBACK_HBM_GBS = 6800.0
 METRIC = "output nnz/s of execute()"
 # Relative error per nonzero against the FP64 numeric model: entries below a
 # floor (a fraction of the container's largest magnitude) are compared against
-# the floor.  The cloth Hessian's coupling entries are sums of terms up to 1e4
-# times the result, so its floor is 1e-4; 1e-10 elsewhere (as in tests/).
+# the floor.  The Hessians' coupling entries (cloth, Neo-Hookean) are sums of
+# terms up to 1e4 times the result, so their floor is 1e-4; 1e-10 elsewhere
+# (as in tests/).
 TOL = 1e-12
-FLOOR = {"cloth": 1e-4}
+FLOOR = {"cloth": 1e-4, "neohookean": 1e-4}
 
 
 def parse():

@@ -579,12 +579,16 @@ CSC<NT> clothMatrix(const ClothRest& r, const std::vector<NT>& X, const std::vec
                         }
                     }
     }
-    forEach(nf, [&](std::size_t fb, std::size_t fe) {
-        for (std::size_t fi = fb; fi < fe; ++fi) {
-            K9s[fi] = {};
-            D9s[fi] = {};
-        }
-    });
+    // With a worker pool, the faces' handles are dropped in parallel too (a
+    // serial loop just lets the vectors go).
+    constexpr bool kPooled = !std::is_same_v<std::decay_t<For>, SerialFor>;
+    if constexpr (kPooled)
+        forEach(nf, [&](std::size_t fb, std::size_t fe) {
+            for (std::size_t fi = fb; fi < fe; ++fi) {
+                K9s[fi] = {};
+                D9s[fi] = {};
+            }
+        });
     K9s.clear();
     D9s.clear();
     // quadratic bend: constant stiffness k Q and damping kd Q per interior edge
@@ -672,10 +676,11 @@ CSC<NT> clothMatrix(const ClothRest& r, const std::vector<NT>& X, const std::vec
             colA[c] = {};
         }
     });
-    for (CSC<NT>* M : {&Kss, &Dss, &Kb, &Db})  // the summands' handles, dropped in parallel too
-        forEach(M->values.size(), [&](std::size_t b, std::size_t e) {
-            for (std::size_t i = b; i < e; ++i) M->values[i] = NT();
-        });
+    if constexpr (kPooled)
+        for (CSC<NT>* M : {&Kss, &Dss, &Kb, &Db})  // the summands' handles, dropped in parallel too
+            forEach(M->values.size(), [&](std::size_t b, std::size_t e) {
+                for (std::size_t i = b; i < e; ++i) M->values[i] = NT();
+            });
     return A;
 }
 

@@ -10,7 +10,8 @@ sys.path.insert(0, str(ROOT))
 GOLDEN = ROOT / "tests" / "golden"
 # (workload, size, seed) of every committed golden fixture (tests/golden/make_golden.sh)
 GOLDEN_CASES = [("ata", 6, 11), ("ata", 9, 12), ("cotan", 5, 21), ("cotan", 8, 22), ("cloth", 3, 31), ("cloth", 5, 32),
-                ("neohookean", 1, 41), ("neohookean", 2, 42)]
+                ("neohookean", 1, 41), ("neohookean", 2, 42), ("cotan", 40, 23), ("cloth", 12, 33),
+                ("neohookean", 4, 43)]
 
 
 def pytest_configure(config):

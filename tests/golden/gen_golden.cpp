@@ -4,6 +4,8 @@
 //   <name>.plan.txt  - the reference's plan for a CUDA device (kernels, templates,
 //                      index/constant/output tables) in the engine's canonical
 //                      plan text;
+//   <name>.refplan   - the same plan as an engine plan file, built from the
+//                      reference's own kernel objects (buildRefPlan below);
 //   <name>.in.bin    - the input values (float64, input containers concatenated);
 //   <name>.out.bin   - the reference CPU ComputeUnit's results (float64), its
 //                      generated code compiled without fast-math or FP
@@ -16,13 +18,16 @@
 #include "SymbolicDifferentiation.hpp"
 #include "SymbolicUtilities.hpp"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <fstream>
 #include <iomanip>
 #include <sstream>
 #include <string>
 
+#include "../../include/symgb.h"
 #include "../../symboliclib_gb300/csrc/workloads/workloads.hpp"
 
 using namespace symgb_workloads;
@@ -51,6 +56,9 @@ SYMREF_EXPOSE(TOutputIdsFlat, &Sym::ComputeUnit<double>::outputIdsFlat)
 SYMREF_EXPOSE(TConstantData, &Sym::ComputeUnit<double>::constantData)
 SYMREF_EXPOSE(TTemplate, &Sym::Kernel::templateExpression)
 SYMREF_EXPOSE(TAccess, &Sym::Kernel::variableAccessData)
+SYMREF_EXPOSE(TOutTable, &Sym::Kernel::outputVariableTable)
+SYMREF_EXPOSE(TVarTable, &Sym::Kernel::variableTable)
+SYMREF_EXPOSE(TConstTable, &Sym::Kernel::constantTable)
 #define REF(obj, TAG) ((obj).*member(TAG{}))
 
 const char* opName(int op) {
@@ -130,6 +138,117 @@ void dumpRefPlan(Sym::ComputeUnit<double>& u, std::ostream& os) {
     os << "\n";
 }
 
+// The reference-side binding of the engine's C ABI: the plan description
+// (symgb_plan_desc) built straight from a reference ComputeUnit's own kernels
+// and tables - the metadata its generated source bakes in as globals
+// (ComputeUnit.cpp:371-407) and the templates its kernel bodies are printed
+// from (ComputeKernel.cpp:329-381) - and written with symgb_plan_save.  This
+// is the code a maintainer adds to ComputeUnit::compile in place of the code
+// generator (INTEGRATION.md shows it as a patch).
+struct RefPlanImage {
+    std::vector<symgb_kernel_desc> kernels;
+    std::vector<std::vector<symgb_node>> nodes;
+    std::vector<std::vector<std::int32_t>> access;
+    std::vector<std::uint64_t> argStart, argLength, outStart, outLength;
+    std::vector<std::uint32_t> index, outIds;
+    std::vector<double> constants;
+    symgb_plan_desc desc{};
+};
+
+void serializeRef(const Sym::Symbolic& x, std::vector<symgb_node>& out) {
+    for (unsigned i = 0; i < x.numChilds(); ++i) serializeRef(x[i], out);
+    symgb_node n{};
+    n.op = x.op();
+    n.nchild = (int)x.numChilds();
+    if (x.op() == Sym::CONST) {
+        n.value = x.constant();
+    } else if (x.op() == Sym::VAR) {
+        n.a = x.variable()[0];
+        n.b = x.variable()[1];
+    }
+    out.push_back(n);
+}
+
+void buildRefPlan(Sym::ComputeUnit<double>& u, RefPlanImage& img) {
+    auto& kernels = REF(u, TKernels);
+    const std::size_t K = kernels.size();
+    img.index.assign(REF(u, TPositionData).begin(), REF(u, TPositionData).end());
+    img.outIds.assign(REF(u, TOutputIdsFlat).begin(), REF(u, TOutputIdsFlat).end());
+    img.constants.assign(REF(u, TConstantData).begin(), REF(u, TConstantData).end());
+    img.kernels.assign(K, symgb_kernel_desc{});
+    img.nodes.resize(K);
+    img.access.resize(K);
+    // Level of each kernel: one more than the deepest kernel whose output
+    // slots it reads (kernels are in topological order), from its index table.
+    std::vector<std::pair<std::uint64_t, std::size_t>> outRanges;  // (first slot, kernel)
+    std::vector<int> level(K, 0);
+    for (std::size_t k = 0; k < K; ++k) {
+        auto& Kr = kernels[k];
+        const std::uint64_t n = (std::uint64_t)Kr.numInstances();
+        symgb_kernel_desc& d = img.kernels[k];
+        d.num_instances = n;
+        d.output_offset = Kr.getGlobalOutputOffset();
+        d.index_offset = Kr.getGlobalIndexOffset();
+        d.constants_offset = Kr.getGlobalConstantsOffset();
+        d.num_output_rows = (std::uint32_t)REF(Kr, TOutTable).size();
+        d.num_index_rows = (std::uint32_t)REF(Kr, TVarTable).size();
+        d.num_constant_rows = (std::uint32_t)REF(Kr, TConstTable).size();
+        serializeRef(REF(Kr, TTemplate), img.nodes[k]);
+        for (auto& a : REF(Kr, TAccess)) {
+            img.access[k].push_back(a.baseVariableId);
+            img.access[k].push_back(a.offset);
+        }
+        int lv = 0;
+        for (auto& a : REF(Kr, TAccess))
+            for (std::uint64_t i = 0; i < n; ++i) {
+                const std::uint64_t slot =
+                    (std::uint32_t)(img.index[d.index_offset + (std::uint64_t)a.baseVariableId * n + i] + a.offset);
+                auto it = std::upper_bound(outRanges.begin(), outRanges.end(),
+                                           std::make_pair(slot, std::numeric_limits<std::size_t>::max()));
+                if (it == outRanges.begin()) continue;  // an input slot
+                --it;
+                const symgb_kernel_desc& p = img.kernels[it->second];
+                if (slot < p.output_offset + p.num_output_rows * p.num_instances) lv = std::max(lv, level[it->second] + 1);
+            }
+        level[k] = lv;
+        d.level = lv;
+        outRanges.insert(std::upper_bound(outRanges.begin(), outRanges.end(), std::make_pair(d.output_offset, k)),
+                         std::make_pair(d.output_offset, k));
+    }
+    for (std::size_t k = 0; k < K; ++k) {
+        img.kernels[k].num_nodes = (std::uint32_t)img.nodes[k].size();
+        img.kernels[k].nodes = img.nodes[k].data();
+        img.kernels[k].num_access = (std::uint32_t)(img.access[k].size() / 2);
+        img.kernels[k].access = img.access[k].data();
+    }
+    std::uint64_t acc = 0;
+    for (auto s : REF(u, TInputSizes)) {
+        img.argStart.push_back(acc);
+        img.argLength.push_back(s);
+        acc += s;
+    }
+    acc = 0;
+    for (auto& ids : REF(u, TOutputIds)) {
+        img.outStart.push_back(acc);
+        img.outLength.push_back(ids.size());
+        acc += ids.size();
+    }
+    symgb_plan_desc& d = img.desc;
+    d.num_kernels = (std::uint32_t)K;
+    d.kernels = img.kernels.data();
+    d.num_args = (std::uint32_t)img.argStart.size();
+    d.arg_start = img.argStart.data();
+    d.arg_length = img.argLength.data();
+    d.num_outputs = (std::uint32_t)img.outStart.size();
+    d.output_start = img.outStart.data();
+    d.output_length = img.outLength.data();
+    d.num_total_memory = REF(u, TInputDataSize) + REF(u, TVariableDataSize);
+    d.num_indices = img.index.size();
+    d.num_output_values = img.outIds.size();
+    d.num_constants = img.constants.size();
+    d.threads_per_block = 128;
+}
+
 void writeBin(const std::string& path, const std::vector<double>& v) {
     std::ofstream f(path, std::ios::binary);
     f.write((const char*)v.data(), v.size() * sizeof(double));
@@ -162,6 +281,13 @@ void run(const std::string& out, const std::vector<Sym::Symbolic>& outputs, cons
                                              inputSyms[1], outputs);
         std::ofstream f(out + ".plan.txt");
         dumpRefPlan(*u, f);
+        RefPlanImage img;
+        buildRefPlan(*u, img);
+        if (symgb_plan_save((out + ".refplan").c_str(), &img.desc, img.index.data(), img.outIds.data(),
+                            img.constants.data()) != 0) {
+            std::fprintf(stderr, "symgb_plan_save: %s\n", symgb_plan_last_error());
+            std::exit(1);
+        }
         // never compiled; not destroyed to keep the process free of dlclose
     }
     Sym::ComputeUnit<double>* cpu = nullptr;
