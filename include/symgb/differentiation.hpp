@@ -17,6 +17,7 @@
 #include <utility>
 #include <vector>
 
+#include "parallel.hpp"
 #include "symbolic.hpp"
 #include "traverse.hpp"
 #include "utilities.hpp"
@@ -134,27 +135,61 @@ inline std::vector<std::vector<Symbolic>> hessianCached(const Symbolic& x, const
 }
 
 // (row, col, expression) entries of the upper triangle of the Hessian of a sum
-// of energies; each summand's Hessian block is made fixed.
+// of energies; each summand's Hessian block is made fixed.  The summands are
+// independent: their blocks are built on the front end's worker pool, the
+// fixed blocks' variables numbered from per-summand counts in summand order
+// (the numbers the summand-by-summand loop gives), and the entries emitted in
+// summand order, so the result does not depend on the thread count.
 inline std::vector<std::tuple<int, int, Symbolic>> hessianSparse(const Symbolic& x, const std::vector<Symbolic>& vars) {
     std::unordered_map<hash_t, std::size_t> varId;
     for (std::size_t i = 0; i < vars.size(); ++i) varId[vars[i].ahash()] = i;
-    std::vector<std::tuple<int, int, Symbolic>> ret;
     if (x.op() != ADD) throw std::invalid_argument("hessianSparse expects a sum of energies");
-    for (const auto& c : x) {
-        std::vector<Symbolic> local;
-        std::vector<std::size_t> ids;
-        for (auto& v : harvestOp(VAR, c)) {
-            auto it = varId.find(v.ahash());
-            if (it != varId.end()) {
-                local.push_back(v);
-                ids.push_back(it->second);
+    const std::size_t n = x.numChilds();
+    std::vector<std::vector<std::vector<Symbolic>>> blocks(n);
+    std::vector<std::vector<std::size_t>> ids(n);
+    std::vector<int> first(n + 1, 0);
+    auto rowSpans = [&](std::size_t t) {
+        std::vector<std::pair<Symbolic*, std::size_t>> d;
+        for (auto& r : blocks[t]) d.emplace_back(r.data(), r.size());
+        return d;
+    };
+    {
+        Symbolic::ConcurrentRefs concurrent;
+        parallelFor(n, 16, [&](std::size_t b, std::size_t e) {
+            for (std::size_t t = b; t < e; ++t) {
+                const Symbolic& c = x[t];
+                std::vector<Symbolic> local;
+                for (auto& v : harvestOp(VAR, c)) {
+                    auto it = varId.find(v.ahash());
+                    if (it != varId.end()) {
+                        local.push_back(v);
+                        ids[t].push_back(it->second);
+                    }
+                }
+                blocks[t] = hessianCached(c, local);
+                first[t + 1] = fixedVariableCount(rowSpans(t));
             }
-        }
-        auto h = hessianCached(c, local);
-        makeFixedRows(h);
-        for (std::size_t i = 0; i < ids.size(); ++i)
-            for (std::size_t j = 0; j < ids.size(); ++j)
-                if (ids[i] <= ids[j]) ret.emplace_back((int)ids[i], (int)ids[j], h[i][j]);
+        });
+        int& counter = Symbolic::uniqueVariableCounter();
+        first[0] = counter;
+        for (std::size_t t = 0; t < n; ++t) first[t + 1] += first[t];
+        parallelFor(n, 16, [&](std::size_t b, std::size_t e) {
+            for (std::size_t t = b; t < e; ++t) makeFixedSpansAt(rowSpans(t), first[t]);
+        });
+        counter = first[n];
+    }
+    std::vector<std::tuple<int, int, Symbolic>> ret;
+    for (std::size_t t = 0; t < n; ++t) {
+        const auto& h = blocks[t];
+        for (std::size_t i = 0; i < ids[t].size(); ++i)
+            for (std::size_t j = 0; j < ids[t].size(); ++j)
+                if (ids[t][i] <= ids[t][j]) ret.emplace_back((int)ids[t][i], (int)ids[t][j], h[i][j]);
+    }
+    {
+        Symbolic::ConcurrentRefs concurrent;
+        parallelFor(n, 256, [&](std::size_t b, std::size_t e) {
+            for (std::size_t t = b; t < e; ++t) blocks[t] = {};
+        });
     }
     return ret;
 }

@@ -790,14 +790,14 @@ std::vector<NT> neoHookeanEnergies(const TetMesh& m, const std::vector<NT>& X) {
 
 // Symmetric Hessian from upper-triangle (row, col, value) entries: each
 // off-diagonal entry is also added transposed, duplicates summed in order.
-template <class NT>
-CSC<NT> symmetricFromUpper(int n, const std::vector<std::tuple<int, int, NT>>& upper) {
+template <class NT, class For = SerialFor>
+CSC<NT> symmetricFromUpper(int n, const std::vector<std::tuple<int, int, NT>>& upper, For&& forEach = For()) {
     std::vector<Triplet<NT>> t;
     t.reserve(2 * upper.size());
     for (const auto& e : upper) t.push_back({std::get<0>(e), std::get<1>(e), std::get<2>(e)});
     for (const auto& e : upper)
         if (std::get<0>(e) != std::get<1>(e)) t.push_back({std::get<1>(e), std::get<0>(e), std::get<2>(e)});
-    return assemble(n, n, t);
+    return assemble(n, n, t, forEach);
 }
 
 // Analytic FP64 Hessian of the same energy (the numeric oracle of workload 5):

@@ -169,7 +169,7 @@ int symgbw_build(const char* name, int size, unsigned long long seed, int vector
             auto XS = variables(X.size(), 0);
             auto E = neoHookeanEnergies(m, XS);
             auto upper = symgb::hessianSparse(symgb::Symbolic(symgb::ADD, E), XS);
-            CSC<symgb::Symbolic> H = symmetricFromUpper((int)X.size(), upper);
+            CSC<symgb::Symbolic> H = symmetricFromUpper((int)X.size(), upper, PoolFor());
             pb.addContainer(XS.data(), XS.size());
             pb.addContainer(H.values.data(), H.values.size());
             w->inputs.push_back(X);

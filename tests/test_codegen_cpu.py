@@ -24,7 +24,7 @@ from symboliclib_gb300 import native
 import oracle.cpu as ocpu
 
 BUILD = ROOT / "symboliclib_gb300" / "_build" / "codegen_tests"
-FAST_FLOOR = {"cloth": 1e-4, "neohookean": 1e-4}
+FAST_FLOOR = {"cloth": 1e-4, "neohookean": 1e-4, "cotan": 1e-4}
 
 HOST_SHIM = r"""
 #include <cmath>

@@ -16,7 +16,7 @@ from symboliclib_gb300 import native
 
 import oracle.cpu as ocpu
 
-FAST_FLOOR = {"cloth": 1e-4, "neohookean": 1e-4}
+FAST_FLOOR = {"cloth": 1e-4, "neohookean": 1e-4, "cotan": 1e-4}
 
 
 def split_inputs(w, flat):
