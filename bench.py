@@ -252,8 +252,22 @@ def run_reference(args):
 
 # Candidates of the on-the-spot tuning (compiled executor): kind, threads per
 # block, items per thread.
-TUNE_SPACE = [("levels", 128, 1), ("levels", 256, 1), ("levels", 128, 2), ("plain", 128, 1), ("plain", 256, 1),
-              ("persistent", 256, 1)]
+TUNE_SPACE = [("plain", 64, 4), ("plain", 128, 2), ("plain", 128, 4), ("levels", 64, 4), ("levels", 128, 1),
+              ("levels", 128, 2), ("levels", 256, 1), ("persistent", 128, 4)]
+
+
+def fp64_instructions(u, tuner, math):
+    """FP64-pipe instructions of one value set, counted from the kernels'
+    programs: one per add, subtract, multiply and FMA; the fast division
+    (two refinement FMAs, a product and two correction FMAs after the
+    approximate reciprocal) 5, the fast square root 6, the fast reciprocal 4
+    (exact mode's IEEE division and square root take more)."""
+    total = 0
+    for k in range(u.num_kernels):
+        sm = tuner.program_summary(u, k, math)
+        per = sm["add"] + sm["sub"] + sm["mul"] + sm["fma"] + 5 * sm["div"] + 6 * sm["sqrt"] + 4 * sm["rec"]
+        total += per * u.kernel_instances[k]
+    return total
 
 
 def main_engine(args):
@@ -382,6 +396,8 @@ def main_engine(args):
     if not args.no_fp64_probe:
         native.check(lib.symgb_measure_fp64_rate(C.byref(fp64)))
     flops_w = (stats.flops + 10 * stats.divs + 10 * stats.sqrts) * S
+    from symboliclib_gb300 import tuner
+    fp64_instr = fp64_instructions(u, tuner, math) * S
     meas = MEASURED.get((args.workload, args.size, S, kind, tpb, items), {})
 
     if rank != 0:
@@ -413,6 +429,10 @@ def main_engine(args):
                      "peak_source": "nominal" if args.no_fp64_probe else "measured",
                      "frac_flop_weighted": flops_w / t_step / fp64.value,
                      "weighting": "add/mul 1, FMA 2, division and square root 10 flops",
+                     "instructions_per_step": fp64_instr,
+                     "pipe_frac_instructions": fp64_instr / t_step / (fp64.value / 2),
+                     "pipe_frac_note": "FP64 instructions the programs issue per step (fast division 5, square "
+                                       "root 6) / step time / the measured FMA rate",
                      "pipe_busy_ncu": meas.get("fp64_pipe_busy"), "profile": meas.get("profile")},
             "clocks": clk.summary()}
     if e2e:
