@@ -24,6 +24,7 @@ with NUMTHREADS = the host's cores; beside it the reference's generated CUDA
 from __future__ import annotations
 
 import argparse
+import atexit
 import ctypes as C
 import json
 import os
@@ -77,48 +78,61 @@ def parse():
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons every 200 ms."""
+    """Clocks and throttle reasons every 200 ms from one long-running
+    `nvidia-smi -lms 200` started before the workload is built (forking a
+    process that holds a large plan can stall the launching thread for a
+    long time; one child started early forks once, while the process is
+    small).  mark_start / mark_stop bound the timed region; the summary uses
+    the samples taken inside it."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
-        self.index, self.rows, self._stop = index, [], threading.Event()
-        self._first = threading.Event()
-        self._t = threading.Thread(target=self._run, daemon=True)
-
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                if out.returncode == 0:
-                    self.rows.append([v.strip() for v in out.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self._first.set()
-            self._stop.wait(0.2)
-
-    def start(self):
-        """Starts sampling and waits (10 s at most) for the first sample, so the
-        sampler's start-up does not fall in a timed region."""
+        self.rows = []  # (time, fields)
+        self.window = (None, None)
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={self.FIELDS}",
+                                        "--format=csv,noheader,nounits", "-lms", "200"],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self._p = None
+        self._t = threading.Thread(target=self._read, daemon=True)
         self._t.start()
-        self._first.wait(timeout=10)
-        return self
+        atexit.register(self.close)
 
-    def stop(self):
-        self._stop.set()
-        self._t.join(timeout=10)
+    def _read(self):
+        if self._p is None:
+            return
+        for line in self._p.stdout:
+            self.rows.append((time.time(), [v.strip() for v in line.strip().split(",")]))
+
+    def mark_start(self):
+        self.window = (time.time(), None)
+
+    def mark_stop(self):
+        time.sleep(0.25)  # one more sample after the region
+        self.window = (self.window[0], time.time())
+
+    def close(self):
+        if self._p is not None and self._p.poll() is None:
+            self._p.terminate()
+            try:
+                self._p.wait(timeout=5)
+            except Exception:
+                self._p.kill()
 
     def summary(self):
-        if not self.rows:
+        t0, t1 = self.window
+        rows = [r for t, r in self.rows if t0 is not None and t1 is not None and t0 <= t <= t1]
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows)}
 
 
 # Per-step DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum over the
@@ -272,6 +286,7 @@ def fp64_instructions(u, tuner, math):
 
 def main_engine(args):
     world, rank, local = dist_init(args)
+    clk = ClockSampler(local)
     import torch
     torch.cuda.set_device(local)
     from symboliclib_gb300 import build, native
@@ -345,7 +360,6 @@ def main_engine(args):
 
     # device-resident timing: L2 cleared (256 MiB write) before every step
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    clk = ClockSampler(local).start()
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             flush.fill_(1.0)
@@ -353,6 +367,7 @@ def main_engine(args):
         torch.cuda.synchronize()
         barrier(world)
         torch.cuda.synchronize()
+        clk.mark_start()
         launches = 0
         for k in range(args.steps):
             flush.fill_(float(k))
@@ -362,7 +377,7 @@ def main_engine(args):
             launches += u.last_launch_count()
         torch.cuda.synchronize()
         barrier(world)
-    clk.stop()
+    clk.mark_stop()
     native.check(lib.symgb_synchronize(u.handle))
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_step = max_over_ranks(world, float(np.mean(step_ms)) * 1e-3)
@@ -435,6 +450,7 @@ def main_engine(args):
                                        "root 6) / step time / the measured FMA rate",
                      "pipe_busy_ncu": meas.get("fp64_pipe_busy"), "profile": meas.get("profile")},
             "clocks": clk.summary()}
+    clk.close()
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu_baseline:

@@ -324,6 +324,13 @@ int symgb_solver_create(int64_t n, const int64_t* col_ptr, const int32_t* row_id
 int symgb_solver_solve(symgb_solver_t s, int method, const double* values, const double* b, double* x, double tol,
                        int max_iter, void* stream, int* iterations, double* max_rel_residual);
 int symgb_solver_multiply(symgb_solver_t s, const double* values, const double* p, double* q, void* stream);
+/* Block-Jacobi preconditioning for BiCGSTAB: the inverses of the b x b
+ * diagonal blocks (b = block_size, 2..4; 1 restores the scaled Jacobi
+ * default) of the unknowns {j b, ..., j b + b - 1} (stride 1) or
+ * {j, j + stride, ..., j + (b - 1) stride} (stride = n / b: each coordinate's
+ * unknowns stored together, e.g. a 3-D mesh's x, y and z rows n / 3 apart).
+ * A block with a zero pivot falls back to the scaled Jacobi of its rows. */
+int symgb_solver_set_block_preconditioner(symgb_solver_t s, int block_size, int64_t stride);
 void symgb_solver_destroy(symgb_solver_t s);
 
 /* Measured FP64 FMA throughput of the current device (FLOP/s, one FMA = 2). */

@@ -1,13 +1,16 @@
-// Batched Jacobi-preconditioned Krylov solves on the device, for the step
+// Batched preconditioned Krylov solves on the device, for the step
 // after assembly: solving A x = b with the cloth system matrix the engine
 // evaluates (reference examples/BaraffWitkin/implementation/cloth.cpp:96-111
 // assembles A = M - h (D + h K) and b; examples/BaraffWitkin/main.cpp:56 keeps
 // its lower triangle, which is what the engine's cloth workload outputs).
 // Conjugate gradient needs A positive definite; the cloth matrices of a
 // stretched and compressed sheet are symmetric but indefinite (negative
-// diagonal entries occur), for which BiCGSTAB is provided.  The preconditioner
-// scales by 1 / |A_ii| (equal to Jacobi for a positive definite A; with the
-// signed diagonal of an indefinite A, BiCGSTAB breaks down).
+// diagonal entries occur), for which BiCGSTAB is provided.  The default
+// preconditioner scales by 1 / |A_ii| (equal to Jacobi for a positive definite
+// A; with the signed diagonal of an indefinite A, BiCGSTAB breaks down);
+// BiCGSTAB can instead use block Jacobi with the exact inverses of the b x b
+// diagonal blocks of one node's unknowns (b = 3 for the cloth: a vertex's x, y
+// and z rows, which the cloth matrix stores n apart).
 //
 // The pattern (lower-triangle or full CSC) is turned once into a full CSR
 // with, per CSR entry, the index of its value in the engine's result buffer.
@@ -278,7 +281,116 @@ __global__ void bFinishStep(const double* __restrict__ ph, const double* __restr
     }
 }
 
+// ---------------------------------------------------------------- block Jacobi
+// Blocks of B unknowns: block j holds rows j * B + a (stride 1, unknowns of one
+// node stored together) or j + a * stride (stride n / B, each coordinate's
+// unknowns stored together, as the cloth matrix orders them).
+
+__device__ __forceinline__ std::uint64_t blockRow(std::uint64_t j, int a, int B, std::uint64_t stride) {
+    return stride == 1 ? j * (std::uint64_t)B + (std::uint64_t)a : j + (std::uint64_t)a * stride;
+}
+
+// inv[(j * B * B + a * B + c) * S + s] = (A_jj^-1)[a][c] of set s, by Gauss-Jordan
+// elimination with partial pivoting; a block with a zero pivot takes the
+// inverse of its absolute diagonal instead (the scaled-Jacobi fallback).
+template <int B>
+__global__ void blockInvert(const double* __restrict__ vals, const std::int64_t* __restrict__ pos, std::uint64_t nb,
+                            unsigned S, double* __restrict__ inv) {
+    const std::uint64_t t = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nb * S) return;
+    const std::uint64_t j = t / S;
+    const unsigned s = (unsigned)(t - j * S);
+    double m[B][2 * B];
+#pragma unroll
+    for (int a = 0; a < B; ++a)
+#pragma unroll
+        for (int c = 0; c < B; ++c) {
+            const std::int64_t e = pos[j * B * B + a * B + c];
+            m[a][c] = e >= 0 ? vals[(std::uint64_t)e * S + s] : 0.0;
+            m[a][B + c] = a == c ? 1.0 : 0.0;
+        }
+    bool singular = false;
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+        int piv = c;
+#pragma unroll
+        for (int a = c + 1; a < B; ++a)
+            if (fabs(m[a][c]) > fabs(m[piv][c])) piv = a;
+        if (m[piv][c] == 0.0) {
+            singular = true;
+            break;
+        }
+#pragma unroll
+        for (int q = 0; q < 2 * B; ++q) {
+            const double tmp = m[c][q];
+            m[c][q] = m[piv][q];
+            m[piv][q] = tmp;
+        }
+        const double d = 1.0 / m[c][c];
+#pragma unroll
+        for (int q = 0; q < 2 * B; ++q) m[c][q] *= d;
+#pragma unroll
+        for (int a = 0; a < B; ++a)
+            if (a != c) {
+                const double f = m[a][c];
+#pragma unroll
+                for (int q = 0; q < 2 * B; ++q) m[a][q] = fma(-f, m[c][q], m[a][q]);
+            }
+    }
+#pragma unroll
+    for (int a = 0; a < B; ++a)
+#pragma unroll
+        for (int c = 0; c < B; ++c) {
+            double v;
+            if (!singular) {
+                v = m[a][B + c];
+            } else {
+                const std::int64_t e = pos[j * B * B + a * B + a];
+                const double d = e >= 0 ? vals[(std::uint64_t)e * S + s] : 0.0;
+                v = a == c ? (d != 0.0 ? 1.0 / fabs(d) : 1.0) : 0.0;
+            }
+            inv[(j * B * B + a * B + c) * S + s] = v;
+        }
+}
+
+// y = M^-1 x with M the block diagonal of A (vectors [row][set]).
+template <int B>
+__global__ void blockApply(const double* __restrict__ inv, const double* __restrict__ x, std::uint64_t n,
+                           std::uint64_t stride, unsigned S, double* __restrict__ y) {
+    const std::uint64_t t = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * S) return;
+    const std::uint64_t i = t / S;
+    const unsigned s = (unsigned)(t - i * S);
+    const std::uint64_t j = stride == 1 ? i / B : i % stride;
+    const int a = stride == 1 ? (int)(i % B) : (int)(i / stride);
+    double acc = 0.0;
+#pragma unroll
+    for (int c = 0; c < B; ++c)
+        acc = fma(inv[(j * B * B + a * B + c) * S + s], x[blockRow(j, c, B, stride) * S + s], acc);
+    y[t] = acc;
+}
+
 unsigned blocksFor(std::uint64_t work) { return (unsigned)((work + kThreads - 1) / kThreads); }
+
+void blockInvertLaunch(int B, const double* vals, const std::int64_t* pos, std::uint64_t nb, unsigned S, double* inv,
+                       cudaStream_t st) {
+    const unsigned g = blocksFor(nb * S);
+    switch (B) {
+        case 2: blockInvert<2><<<g, kThreads, 0, st>>>(vals, pos, nb, S, inv); break;
+        case 3: blockInvert<3><<<g, kThreads, 0, st>>>(vals, pos, nb, S, inv); break;
+        default: blockInvert<4><<<g, kThreads, 0, st>>>(vals, pos, nb, S, inv); break;
+    }
+}
+
+void blockApplyLaunch(int B, const double* inv, const double* x, std::uint64_t n, std::uint64_t stride, unsigned S,
+                      double* y, cudaStream_t st) {
+    const unsigned g = blocksFor(n * S);
+    switch (B) {
+        case 2: blockApply<2><<<g, kThreads, 0, st>>>(inv, x, n, stride, S, y); break;
+        case 3: blockApply<3><<<g, kThreads, 0, st>>>(inv, x, n, stride, S, y); break;
+        default: blockApply<4><<<g, kThreads, 0, st>>>(inv, x, n, stride, S, y); break;
+    }
+}
 
 }  // namespace
 
@@ -289,6 +401,13 @@ struct symgb_solver {
     symgb::engine::DevBuf<int> col;
     symgb::engine::DevBuf<double> vals, x, r, p, q, invDiag, scalars, rhat, v, ph, sv, sh, t;
     double* hostScalars = nullptr;  // pinned copy of rr and bb
+    // Host copy of the full CSR (block positions) and the block preconditioner.
+    std::vector<std::int64_t> rowPtrHost;
+    std::vector<int> colHost;
+    int block = 1;                  // unknowns per block (1: scaled Jacobi)
+    std::uint64_t blockStride = 1;  // 1: contiguous blocks; n / block: one unknown per coordinate group
+    symgb::engine::DevBuf<std::int64_t> blockPos;
+    symgb::engine::DevBuf<double> blockInv;
     ~symgb_solver() {
         if (hostScalars) cudaFreeHost(hostScalars);
     }
@@ -350,7 +469,42 @@ int symgb_solver_create(int64_t n, const int64_t* col_ptr, const int32_t* row_id
     if (!col.empty()) cudaMemcpy(s->col.ptr, col.data(), col.size() * 4, cudaMemcpyHostToDevice);
     cudaMemcpy(s->diagPos.ptr, diag.data(), diag.size() * 8, cudaMemcpyHostToDevice);
     if (cudaGetLastError() != cudaSuccess) return fail("upload failed");
+    s->rowPtrHost = std::move(rowPtr);
+    s->colHost = std::move(col);
     *out = s;
+    return SYMGB_OK;
+}
+
+int symgb_solver_set_block_preconditioner(symgb_solver_t s, int block_size, int64_t stride) {
+    using symgb::engine::setLastError;
+    if (!s || block_size < 1 || block_size > 4) return setLastError(SYMGB_ERR_ARGUMENT, "solver: block size 1..4");
+    if (block_size == 1) {
+        s->block = 1;
+        return SYMGB_OK;
+    }
+    const std::uint64_t n = s->n, B = (std::uint64_t)block_size;
+    if (n % B) return setLastError(SYMGB_ERR_ARGUMENT, "solver: unknowns not a multiple of the block size");
+    if (stride != 1 && (std::uint64_t)stride * B != n)
+        return setLastError(SYMGB_ERR_ARGUMENT, "solver: stride must be 1 or n / block_size");
+    const std::uint64_t nb = n / B;
+    auto row = [&](std::uint64_t j, std::uint64_t a) { return stride == 1 ? j * B + a : j + a * (std::uint64_t)stride; };
+    std::vector<std::int64_t> pos(nb * B * B, -1);
+    for (std::uint64_t j = 0; j < nb; ++j)
+        for (std::uint64_t a = 0; a < B; ++a) {
+            const std::uint64_t r = row(j, a);
+            const int* b = s->colHost.data() + s->rowPtrHost[r];
+            const int* e = s->colHost.data() + s->rowPtrHost[r + 1];
+            for (std::uint64_t c = 0; c < B; ++c) {
+                const int* f = std::lower_bound(b, e, (int)row(j, c));
+                if (f != e && *f == (int)row(j, c)) pos[(j * B + a) * B + c] = (std::int64_t)(f - s->colHost.data());
+            }
+        }
+    if (s->blockPos.alloc(pos.size()) || s->blockInv.alloc(pos.size() * s->S))
+        return setLastError(SYMGB_ERR_NOMEM, "solver: device allocation failed");
+    if (cudaMemcpy(s->blockPos.ptr, pos.data(), pos.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+        return setLastError(SYMGB_ERR_CUDA, "solver: upload failed");
+    s->block = block_size;
+    s->blockStride = (std::uint64_t)stride;
     return SYMGB_OK;
 }
 
@@ -453,6 +607,8 @@ static int solveBicgstab(symgb_solver_t s, const double* values, const double* b
     cudaMemsetAsync(s->scalars.ptr, 0, 16 * (std::size_t)S * sizeof(double), st);
     bStart<<<blocksFor(work), kThreads, smem1, st>>>(b_dev, s->vals.ptr, s->diagPos.ptr, s->n, S, s->x.ptr, s->r.ptr,
                                                     s->rhat.ptr, s->p.ptr, s->v.ptr, s->invDiag.ptr, R, bb);
+    const bool blocks = s->block > 1;
+    if (blocks) blockInvertLaunch(s->block, s->vals.ptr, s->blockPos.ptr, s->n / s->block, S, s->blockInv.ptr, st);
     {
         std::vector<double> ones(3 * (std::size_t)S, 1.0);  // R[2] (previous rho), alpha, omega = 1
         cudaMemcpyAsync(R + 2 * S, ones.data(), S * sizeof(double), cudaMemcpyHostToDevice, st);
@@ -473,10 +629,12 @@ static int solveBicgstab(symgb_solver_t s, const double* values, const double* b
             cudaMemsetAsync(rhoNext, 0, S * sizeof(double), st);
             bDirection<<<blocksFor(work), kThreads, 0, st>>>(s->r.ptr, s->v.ptr, s->invDiag.ptr, s->n, S, rho, rhoPrev,
                                                             alpha, omega, s->p.ptr, s->ph.ptr);
+            if (blocks) blockApplyLaunch(s->block, s->blockInv.ptr, s->p.ptr, s->n, s->blockStride, S, s->ph.ptr, st);
             bSpmv<<<blocksFor(work), kThreads, smem2, st>>>(s->rowPtr.ptr, s->col.ptr, s->vals.ptr, s->ph.ptr, s->n, S,
                                                            s->rhat.ptr, s->v.ptr, rv, nullptr);
             bHalf<<<blocksFor(work), kThreads, 0, st>>>(s->r.ptr, s->v.ptr, s->invDiag.ptr, s->n, S, rho, rv, alpha,
                                                        s->sv.ptr, s->sh.ptr);
+            if (blocks) blockApplyLaunch(s->block, s->blockInv.ptr, s->sv.ptr, s->n, s->blockStride, S, s->sh.ptr, st);
             bSpmv<<<blocksFor(work), kThreads, smem2, st>>>(s->rowPtr.ptr, s->col.ptr, s->vals.ptr, s->sh.ptr, s->n, S,
                                                            s->sv.ptr, s->t.ptr, ts, tt);
             bFinishStep<<<blocksFor(work), kThreads, smem2, st>>>(s->ph.ptr, s->sh.ptr, s->sv.ptr, s->t.ptr,

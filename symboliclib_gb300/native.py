@@ -84,6 +84,7 @@ SYMGB_FUNCTIONS = {
                                      C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "symgb_solver_multiply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "symgb_solver_destroy": (None, [C.c_void_p]),
+    "symgb_solver_set_block_preconditioner": (C.c_int, [C.c_void_p, C.c_int, C.c_int64]),
     "symgb_time_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_double)]),
     "symgb_plan_save": (C.c_int, [C.c_char_p, C.POINTER(PlanDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
     "symgb_plan_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
@@ -298,6 +299,10 @@ class SparseSolver:
         check(self._lib.symgb_solver_solve(self.handle, method, C.c_void_p(values.data_ptr()), C.c_void_p(b.data_ptr()),
                                            C.c_void_p(x.data_ptr()), tol, max_iter, st, C.byref(it), C.byref(res)))
         return it.value, res.value
+
+    def set_block_preconditioner(self, block_size: int, stride: int) -> None:
+        """BiCGSTAB with block Jacobi (symgb_solver_set_block_preconditioner)."""
+        check(self._lib.symgb_solver_set_block_preconditioner(self.handle, block_size, stride))
 
     def multiply(self, values, p, q, stream=None) -> None:
         st = C.c_void_p(stream.cuda_stream) if stream is not None else None
