@@ -72,7 +72,7 @@ def single(args):
     # plain per-call path: one value set, one launch per kernel
     for i, a in enumerate(w.inputs):
         u.set_arg(i, a)
-    plain = tuner.Sched("plain", 1, 128, 1)
+    plain = tuner.Sched("plain", 1, 128, 1, 1, "compiled")
     plain.apply(u, graph=0)
     u.run()
     err_plain = rel_err(u.get_result(0), w.numeric)
@@ -151,17 +151,20 @@ def batch(args):
         if key not in plain_by_side:
             for i, a in enumerate(w.inputs):
                 u.set_arg(i, a)
-            plain_by_side[key] = tuner.time_schedule(u, tuner.Sched("plain", 1, 128, 1), stream, None, runs=5) * 1e-6
+            plain_by_side[key] = tuner.time_schedule(u, tuner.Sched("plain", 1, 128, 1, 1, "compiled"), stream, None,
+                                                     runs=5) * 1e-6
         plain_s += plain_by_side[key] * S
     # batched: each unit with its sets, tuned schedule choice per unit size class, one graph
     for u, S, w in units:
         u.set_num_sets(S)
         for i, a in enumerate(w.inputs):
             u.set_arg(i, np.tile(a, S))
-        tuner.Sched(args.schedule, args.items, args.tpb, 1, args.lanes).apply(u, graph=0)
+        tuner.Sched(args.schedule, args.items, args.tpb, 1, args.lanes, args.executor).apply(u, graph=0)
     handles = (C.c_void_p * len(units))(*[u.handle.value for u, _, _ in units])
     b = C.c_void_p()
+    t_create = time.perf_counter()
     native.check(lib.symgb_batch_create(handles, len(units), args.streams, C.byref(b)))
+    create_s = time.perf_counter() - t_create
     for _ in range(3):
         native.check(lib.symgb_batch_run(b))
     ts = []
@@ -185,8 +188,9 @@ def batch(args):
         "instances": int(args.count), "sides": [int(sides.min()), int(sides.max())], "distinct_patterns": len(cache),
         "value_sets_total": int(sets.sum()), "output_nnz_total": int(total_nnz), "front_end_s": round(front, 1),
         "graph": {"ms": t_graph * 1e3, "nnz_per_s": total_nnz / t_graph, "kernels": int(launches),
-                  "streams": args.streams, "schedule": f"{args.schedule} items {args.items} lanes {args.lanes} "
-                                                        f"tpb {args.tpb}"},
+                  "streams": args.streams, "schedule": f"{args.executor} {args.schedule} items {args.items} "
+                                                        f"lanes {args.lanes} tpb {args.tpb}",
+                  "create_s": round(create_s, 1)},
         "plain_per_call": {"ms": plain_s * 1e3, "nnz_per_s": total_nnz / plain_s},
         "speedup": plain_s / t_graph, "max_rel_err_sampled": max(errs)}), flush=True)
 
@@ -218,16 +222,27 @@ def learned(args):
     t_fit = time.perf_counter()
     loss = model.fit(np.stack(X), np.array(y), epochs=args.epochs)
     t_fit = time.perf_counter() - t_fit
+    t_front = time.perf_counter()
     w = native.Workload(args.target, args.target_size, args.seed)
+    t_front = time.perf_counter() - t_front
     u = native.Unit.from_workload(w)
+    S = args.target_sets
+    u.set_num_sets(S)
     for i, a in enumerate(w.inputs):
-        u.set_arg(i, a)
+        u.set_arg(i, np.tile(a, S))
     stream = tuner.bind_stream(u)
     flush = flush_buffer()
-    full = tuner.exhaustive(u, stream, flush, runs=5)
+    # the learned proposal first, so its compiles are not served from the
+    # exhaustive pass's module cache
     prop = tuner.tune_with_model(u, model, stream, flush, k=args.k, runs=5)
+    full = tuner.exhaustive(u, stream, flush, runs=5)
+    prop.best.apply(u)
+    u.run()
+    err = rel_err(u.get_result(0).reshape(S, -1)[0], w.numeric)
     print(json.dumps({
-        "target": f"{args.target} {args.target_size}", "output_nnz": len(w.numeric),
+        "target": f"{args.target} {args.target_size}", "output_nnz": len(w.numeric), "value_sets": S,
+        "front_end_s": round(t_front, 1), "max_rel_err_vs_fp64_model": err,
+        "learned_nnz_per_s": len(w.numeric) * S / (full.timings.get(prop.best, prop.best_us) * 1e-6),
         "training_samples": len(y), "training_units": len(train), "collect_s": round(t_collect, 1),
         "fit_s": round(t_fit, 2), "fit_mse_log": loss,
         "exhaustive": {"best": str(full.best), "best_us": full.best_us, "timed": full.timed, "seconds": full.seconds},
@@ -321,6 +336,8 @@ def solve(args):
     b = torch.from_numpy(rng.standard_normal((S, r))).cuda()
     x = torch.empty_like(b)
     solver = native.SparseSolver(r, cp, ri, True, S)
+    if args.block > 1:
+        solver.set_block_preconditioner(args.block, r // args.block)
     method = native.SOLVER_BICGSTAB if args.method == "bicgstab" else native.SOLVER_CG
     solver.solve(vals, b, x, args.tol, 20, method)  # warm-up
     torch.cuda.synchronize()
@@ -348,7 +365,8 @@ def solve(args):
     t_cpu = time.perf_counter() - t1
     resid = float(np.linalg.norm(A @ x[0].cpu().numpy() - bh) / np.linalg.norm(bh))
     print(json.dumps({
-        "workload": f"cloth {args.size}", "unknowns": r, "nnz_lower": nnz, "nnz_full": nnz_full, "systems": S,
+        "workload": f"cloth {args.size}", "preconditioner": f"block Jacobi {args.block}x{args.block}"
+        if args.block > 1 else "scaled Jacobi", "unknowns": r, "nnz_lower": nnz, "nnz_full": nnz_full, "systems": S,
         "gpu": {"iterations": it, "max_rel_residual": res, "seconds": t, "us_per_iteration": t / max(1, it) * 1e6,
                 "bytes_per_iteration": per_iter_bytes, "hbm_gbs": per_iter_bytes * it / t / 1e9,
                 "hbm_frac": per_iter_bytes * it / t / 1e9 / hbm_peak(), "checked_residual_set0": resid},
@@ -375,13 +393,15 @@ def main():
     b.add_argument("--streams", type=int, default=8)
     b.add_argument("--schedule", default="levels", choices=list(tuner.KINDS))
     b.add_argument("--items", type=int, default=1)
-    b.add_argument("--lanes", type=int, default=2)
+    b.add_argument("--lanes", type=int, default=1)
+    b.add_argument("--executor", default="compiled", choices=["compiled", "interpreter"])
     b.add_argument("--tpb", type=int, default=64)
     b.add_argument("--seed", type=int, default=7)
     b.add_argument("--steps", type=int, default=10)
     c = sub.add_parser("learned")
     c.add_argument("--target", default="neohookean")
     c.add_argument("--target-size", type=int, default=6)
+    c.add_argument("--target-sets", type=int, default=1)
     c.add_argument("--k", type=int, default=len(tuner.SPACE) // 15)
     c.add_argument("--epochs", type=int, default=4000)
     c.add_argument("--seed", type=int, default=5)
@@ -399,6 +419,7 @@ def main():
     e.add_argument("--max-iter", type=int, default=5000)
     e.add_argument("--seed", type=int, default=3)
     e.add_argument("--method", default="bicgstab", choices=["cg", "bicgstab"])
+    e.add_argument("--block", type=int, default=3, help="block-Jacobi block size (1: scaled Jacobi)")
     args = ap.parse_args()
     {"single": single, "batch": batch, "learned": learned, "kernels": kernels, "solve": solve}[args.cmd](args)
 
