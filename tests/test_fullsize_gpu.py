@@ -13,8 +13,9 @@
 * an uneven multi-pattern batch (cloth sides drawn log-uniform, 1 to 16 value
   sets each) in one graph replay: every unit bit-identical to the oracle.
 * Neo-Hookean 10^3 cells: exact mode bit-identical to the oracle.
-* the engine front end's tables at these sizes equal the reference's own
-  (SHA-256 digests recorded in tests/golden/reference_tables.json by
+* the engine front end's tables equal the reference's own at cotan 500x500
+  and cloth 200x200, in the CUDA and the CPU (VecWidth(4)) layouts (SHA-256
+  digests recorded in tests/golden/reference_tables.json by
   tests/golden/make_table_hashes.py from the files the reference wrote);
 * the reference's own generated CUDA, where oracle/ref_generate.sh kept it,
   built with --fmad=false: bit-identical to the engine's exact mode; its
@@ -72,6 +73,11 @@ def cloth300():
 
 
 @pytest.fixture(scope="module")
+def cloth200():
+    return native.Workload("cloth", 200, 2024)
+
+
+@pytest.fixture(scope="module")
 def cotan500_oracle(cotan500):
     w = cotan500
     return ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
@@ -81,11 +87,14 @@ def test_cotan500_tables_equal_reference(cotan500):
     check_tables(cotan500, "cotan_500_cuda")
 
 
-def test_cloth300_tables_equal_reference(cloth300):
-    check_tables(cloth300, "cloth_300_cuda")
+def test_cloth200_tables_equal_reference(cloth200):
+    """cloth 200x200 is the largest cloth whose reference plan fits the 62 GB
+    host the fixtures were generated on (the reference's front end needs more
+    than that for 300x300)."""
+    check_tables(cloth200, "cloth_200_cuda")
 
 
-@pytest.mark.parametrize("name,size", [("cotan", 500), ("cloth", 300)])
+@pytest.mark.parametrize("name,size", [("cotan", 500), ("cloth", 200)])
 def test_cpu_layout_tables_equal_reference(name, size):
     """The reference CPU ComputeUnit's layout (VecWidth(4): padded, blocked
     tables) from the engine's front end, against the reference's own."""
@@ -192,15 +201,15 @@ def test_neohookean_10_exact():
             assert bits_equal(u.get_result(0), ref), (executor, kind)
 
 
-@pytest.mark.parametrize("name,size", [("cotan", 500), ("cloth", 300)])
-def test_reference_generated_cuda_matches_engine(name, size, cotan500, cloth300, tmp_path):
+@pytest.mark.parametrize("name,size", [("cotan", 500), ("cloth", 200)])
+def test_reference_generated_cuda_matches_engine(name, size, cotan500, cloth200, tmp_path):
     """The reference's generated CUDA for one value set, built by its own nvcc
     command with -arch=sm_103a --fmad=false, equals the engine's exact mode
     bit for bit; its default build (FMA contraction by nvcc) is within the
     fast-mode tolerance of it."""
     if not ref_paths.available(name, size, "cuda"):
         pytest.skip("the reference's generated code was not kept (oracle/ref_generate.sh)")
-    w = cotan500 if name == "cotan" else cloth300
+    w = cotan500 if name == "cotan" else cloth200
     res = ref_paths.gpu_paths(name, size, warmup=1, steps=3, results_dir=tmp_path)
     assert res["ref_exact"]["outputs"] == len(w.numeric)
     u = native.Unit.from_workload(w)
