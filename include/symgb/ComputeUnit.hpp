@@ -58,7 +58,8 @@ struct PersistentSchedule {};
 class Device {
 public:
     unsigned vectorWidth = 1;
-    unsigned numThreads = 1;
+    unsigned numThreads = 1;        // NumThreads: host threads of a CPU device
+    unsigned threadsPerBlock = 0;   // ThreadsPerBlock: CUDA block size (0: engine default)
     unsigned decompositionThreshold = 6;
     bool singlePrecision = false;
     bool cudaDevice = false;
@@ -75,7 +76,13 @@ public:
 
 private:
     void set(const DecompositionThreshold& v) { decompositionThreshold = (unsigned)v.x; }
-    void set(const ThreadsPerBlock& v) { numThreads = (unsigned)v.x; }
+    // The engine's kernels work in whole warps: a block size that is not a
+    // multiple of 32 in [32, 1024] is rejected rather than rounded.
+    void set(const ThreadsPerBlock& v) {
+        if (v.x < 32 || v.x > 1024 || v.x % 32)
+            throw std::invalid_argument("ThreadsPerBlock: the engine needs a multiple of 32 in [32, 1024]");
+        threadsPerBlock = (unsigned)v.x;
+    }
     void set(const VecWidth& v) { vectorWidth = (unsigned)v.x; }
     void set(const NumThreads& v) { numThreads = (unsigned)v.x; }
     void set(const ValueSets& v) { valueSets = v.x; }
@@ -137,7 +144,7 @@ public:
         PlanBuilder pb(cfg);
         (pb.addContainer(detail::contPtr(const_cast<Containers&>(containers)), detail::contSize(containers)), ...);
         plan_ = pb.build();
-        buildPlanImage(plan_, image_, device.numThreads ? device.numThreads : 128);
+        buildPlanImage(plan_, image_, device.threadsPerBlock ? device.threadsPerBlock : 128);
     }
 
     ComputeUnit(const ComputeUnit&) = delete;
@@ -149,15 +156,17 @@ public:
     ComputeUnit& compile() {
         close();
         check(symgb_unit_create(&image_.desc, &unit_));
-        symgb_schedule s{device_.schedule, device_.math, (int)(device_.numThreads % 32 ? 0 : device_.numThreads), 0, 0, 0,
-                         device_.itemsPerThread, 0};
+        symgb_schedule s{device_.schedule, device_.math, (int)device_.threadsPerBlock, 0, 0, 0, device_.itemsPerThread, 0};
         check(symgb_set_schedule(unit_, &s));
         check(symgb_set_num_sets(unit_, device_.valueSets));
         check(symgb_init(unit_, image_.indexData.data(), image_.outIndexData.data(), image_.constData.data()));
         return *this;
     }
 
-    // setArg for every input container, then run().
+    // setArg for every input container, then run().  Synchronous copies from
+    // the containers' own memory; containers that are page-locked
+    // (cudaHostRegister) are copied by DMA at full link speed.  Overlapped
+    // copies are the C ABI's *_async calls.
     template <class... Values>
     ComputeUnit& execute(const Values&... values) {
         requireCompiled();

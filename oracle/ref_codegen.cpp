@@ -1,7 +1,7 @@
 // Runs the reference SymbolicLib front end (oracle/_ref/libsymref.so, built
 // from the reference's own sources by oracle/Makefile) on one of the project's
 // synthetic workloads and keeps what its ComputeUnit generates, so that the
-// reference's own execution paths can be compiled and timed on the GPU host:
+// reference's own execution paths can be compiled and timed next to the GPU:
 //
 //   cuda: cudaCode.cu   - the reference's generated CUDA source for
 //                         Device(UseCuda(), ThreadsPerBlock(tpb))

@@ -3,7 +3,7 @@
 # workloads in oracle/_ref/gen/<workload>_<size>_<cuda|cpu>/ (see
 # oracle/ref_paths.py).  Needs the reference sources (REF, default
 # /root/reference) to build oracle/_ref/libsymref.so; run where they are
-# mounted, before the directories are taken to the GPU host.
+# mounted, before the directories are taken to the machine with the GPU.
 #
 #   oracle/ref_generate.sh [workload:size:seed ...]
 #   (default: cotan:500:2024 cloth:300:2024, both devices)

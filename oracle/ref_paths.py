@@ -8,7 +8,7 @@ writes: its generated source (cudaCode.cu for Device(UseCuda(),
 ThreadsPerBlock(128)), cpuCode.cpp for Device(VecWidth(4))), its table files
 (indexData, constData, outIndexData) and the inputs, in
 oracle/_ref/gen/<workload>_<size>_<cuda|cpu>/.  Those directories travel to
-the GPU host, where oracle/ref_paths.sh compiles the sources (the reference's
+the machine with the GPU, where oracle/ref_paths.sh compiles the sources (the reference's
 own nvcc / clang++ command lines; g++ stands in for clang++) and
 oracle/ref_run.cpp loads the library through the reference's five calls and
 times it.  bench.py uses this for its reference arm (the CPU ComputeUnit) and

@@ -1,7 +1,7 @@
 #!/bin/sh
 # Builds the reference's own execution paths for one workload from the source
 # its ComputeUnit generated (oracle/ref_codegen.cpp keeps it in <gen_dir>), and
-# the timing driver oracle/ref_run.cpp.  Runs on the GPU host (aarch64): no
+# the timing driver oracle/ref_run.cpp.  Runs next to the GPU (aarch64 too): no
 # file of the reference is needed there, only <gen_dir>.
 #
 #   oracle/ref_paths.sh <gen_dir> cuda     # cudaCode.cu ->

@@ -41,6 +41,14 @@ int main(int argc, char** argv) {
     ComputeUnit<double> unit(Device(UseCuda(), ThreadsPerBlock(128)), AS, BS.values);
     const std::size_t nk = unit.planDesc().num_kernels;
     expect(nk > 0, "kernels planned", (double)nk, 1.0);
+    // a block size the engine cannot honour is an error, not silently replaced
+    bool rejected = false;
+    try {
+        Device bad(UseCuda(), ThreadsPerBlock(100));
+    } catch (const std::invalid_argument&) {
+        rejected = true;
+    }
+    expect(rejected, "ThreadsPerBlock(100) rejected", rejected, 1.0);
     if (gpu) {
         std::vector<double> B(BS.nnz(), 0.0);
         unit.compile().execute(A.values).getResults(B);
