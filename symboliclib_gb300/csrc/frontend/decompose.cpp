@@ -13,6 +13,7 @@
 #include <set>
 #include <unordered_map>
 
+#include "symgb/stage_clock.hpp"
 #include "symgb/frontend.hpp"
 #include "symgb/parallel.hpp"
 #include "symgb/traverse.hpp"
@@ -174,6 +175,7 @@ std::vector<ExpressionBlock> decompose(const std::vector<Symbolic>& expr, unsign
         return ret;
     }
 
+    StageClock clock;
     std::vector<Node> nodes;
     nodes.reserve(5 * expr.size());
     // node identity -> (occurrence count, node index + 1)
@@ -201,6 +203,8 @@ std::vector<ExpressionBlock> decompose(const std::vector<Symbolic>& expr, unsign
             return xc.first++ == 0;
         });
     }
+
+    clock.mark("decompose: count");
 
     // 2. One node per output expression.
     std::vector<unsigned> outputNodes;
@@ -245,6 +249,7 @@ std::vector<ExpressionBlock> decompose(const std::vector<Symbolic>& expr, unsign
     });
     for (auto& node : nodes)
         for (auto& c : node.childs) ++c.second->numParents;
+    clock.mark("decompose: links");
 
     // 4. Merge small and single-parent children, assign levels.  `reachable`
     // is a flag per node; nodes live in one array, so index order is the
@@ -291,6 +296,8 @@ std::vector<ExpressionBlock> decompose(const std::vector<Symbolic>& expr, unsign
         }
     }
 
+    clock.mark("decompose: merge, levels");
+
     // 5. Blocks of the reachable, non-inlined nodes in node order.  Each
     // block's extraction only reads the node graph, so blocks are extracted
     // in parallel (reference counts atomic meanwhile).
@@ -319,6 +326,7 @@ std::vector<ExpressionBlock> decompose(const std::vector<Symbolic>& expr, unsign
     }
     for (auto& b : blocks)
         for (auto& c : b.childs) c = blockIdMap[c];
+    clock.mark("decompose: extract");
     return blocks;
 }
 

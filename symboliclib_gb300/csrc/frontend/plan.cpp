@@ -11,6 +11,7 @@
 
 #include "symgb/frontend.hpp"
 #include "symgb/parallel.hpp"
+#include "symgb/stage_clock.hpp"
 #include "symgb/traverse.hpp"
 
 namespace symgb {
@@ -67,8 +68,10 @@ void PlanBuilder::addContainer(const Symbolic* expr, std::size_t len) {
 Plan PlanBuilder::build() {
     Plan& P = plan_;
     const DeviceConfig& dev = P.device;
+    StageClock clock;
     std::vector<ExpressionBlock> blocks =
         decompose(outputExpressions_, (unsigned char)dev.decompositionThreshold, GLOBAL_INTERMEDIATE, true);
+    clock.mark("decompose (total)");
 
     // Group blocks by (structure hash, level) in first-seen order (ComputeUnit.cpp:34-56).
     std::unordered_map<hash_t, int> groupMap;
@@ -120,6 +123,8 @@ Plan PlanBuilder::build() {
         }
     }
 
+    clock.mark("kernels");
+
     // Execution order: children before parents (ComputeUnit.cpp:279-296).
     std::vector<std::set<int>> deps(kernels.size());
     for (int i = 0; i < (int)blocks.size(); ++i)
@@ -163,6 +168,8 @@ Plan PlanBuilder::build() {
         const auto& cd = k.constantData();
         P.constantData.insert(P.constantData.end(), cd.begin(), cd.end());
     }
+
+    clock.mark("order, layout");
 
     // Index table: every kernel's variable slots, filled in parallel (the maps
     // are only read here).  An input group without an offset reads from 0.
@@ -210,6 +217,7 @@ Plan PlanBuilder::build() {
     }
     P.inputDataSize = inputDataSize_;
     P.numTotalMemory = inputDataSize_ + variableDataSize;
+    clock.mark("index table");
 
     // The blocks' expressions are released in parallel (most of their nodes
     // belong to one block; reference counts are atomic meanwhile).
@@ -226,6 +234,7 @@ Plan PlanBuilder::build() {
         });
     }
     outputExpressions_.clear();
+    clock.mark("release");
     return std::move(plan_);
 }
 

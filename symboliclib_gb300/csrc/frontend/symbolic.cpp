@@ -50,20 +50,29 @@ long long& liveNodes() {
 }
 
 // Nodes are small and created by the million; a per-thread free list keeps
-// allocation off the general-purpose heap.
+// allocation off the general-purpose heap.  The list is threaded through the
+// free nodes themselves (the link lives in the union of a dead node), so
+// freeing the hundreds of millions of nodes of a large expression graph
+// touches no other memory.
 struct NodePool {
-    std::vector<Symbolic::Node*> freeList;
+    Symbolic::Node* head = nullptr;
+    static Symbolic::Node*& link(Symbolic::Node* p) { return *reinterpret_cast<Symbolic::Node**>(&p->childs); }
     Symbolic::Node* get() {
-        if (freeList.empty()) {
+        if (!head) {
             const std::size_t n = 4096;
             auto* slab = static_cast<Symbolic::Node*>(std::malloc(n * sizeof(Symbolic::Node)));
-            for (std::size_t i = 0; i < n; ++i) freeList.push_back(slab + (n - 1 - i));
+            if (!slab) throw std::bad_alloc();
+            for (std::size_t i = 0; i < n; ++i) link(slab + i) = i + 1 < n ? slab + i + 1 : nullptr;
+            head = slab;
         }
-        Symbolic::Node* p = freeList.back();
-        freeList.pop_back();
+        Symbolic::Node* p = head;
+        head = link(p);
         return p;
     }
-    void put(Symbolic::Node* p) { freeList.push_back(p); }
+    void put(Symbolic::Node* p) {
+        link(p) = head;
+        head = p;
+    }
 };
 
 // One global pool guarded by a mutex would serialise the front end; nodes are
@@ -76,22 +85,29 @@ NodePool& pool() {
 }
 
 // Child arrays of up to kPooledChilds handles come from per-size free lists
-// (same ownership rules as nodes); longer arrays use new[].
+// (same ownership rules as nodes, linked through their first handle's
+// storage); longer arrays use new[].
 constexpr unsigned kPooledChilds = 8;
 struct ChildPool {
-    std::vector<void*> freeList[kPooledChilds + 1];
+    void* head[kPooledChilds + 1] = {};
+    static void*& link(void* p) { return *static_cast<void**>(p); }
     void* get(unsigned n) {
-        auto& f = freeList[n];
-        if (f.empty()) {
-            const std::size_t count = 2048;
-            char* slab = static_cast<char*>(std::malloc(count * n * sizeof(Symbolic)));
-            for (std::size_t i = 0; i < count; ++i) f.push_back(slab + (count - 1 - i) * n * sizeof(Symbolic));
+        void*& h = head[n];
+        if (!h) {
+            const std::size_t count = 2048, bytes = n * sizeof(Symbolic);
+            char* slab = static_cast<char*>(std::malloc(count * bytes));
+            if (!slab) throw std::bad_alloc();
+            for (std::size_t i = 0; i < count; ++i) link(slab + i * bytes) = i + 1 < count ? slab + (i + 1) * bytes : nullptr;
+            h = slab;
         }
-        void* p = f.back();
-        f.pop_back();
+        void* p = h;
+        h = link(p);
         return p;
     }
-    void put(void* p, unsigned n) { freeList[n].push_back(p); }
+    void put(void* p, unsigned n) {
+        link(p) = head[n];
+        head[n] = p;
+    }
 };
 
 ChildPool& childPool() {
