@@ -500,18 +500,26 @@ def end_to_end(args, w, u, make_unit, apply, sched, inputs, nnz, S, floor, world
         native.check(lib.symgb_run_async(uu.handle))
         native.check(lib.symgb_get_result_sets_async(uu.handle, C.c_void_p(pin_o.data_ptr()), 0))
 
-    for k in range(4):
-        step(k)
-    for uu, _, _ in pipe:
-        native.check(lib.symgb_synchronize(uu.handle))
-    barrier(world)
-    t0 = time.perf_counter()
-    for k in range(steps):
-        step(k)
-    for uu, _, _ in pipe:
-        native.check(lib.symgb_synchronize(uu.handle))
-    t_e2e = max_over_ranks(world, (time.perf_counter() - t0) / steps)
-    barrier(world)
+    # the result copy on 1 or 4 copy streams (several copy engines), the
+    # faster one reported
+    by_streams = {}
+    for cs in (1, 4):
+        for uu, _, _ in pipe:
+            uu.set_copy_streams(cs)
+        for k in range(4):
+            step(k)
+        for uu, _, _ in pipe:
+            native.check(lib.symgb_synchronize(uu.handle))
+        barrier(world)
+        t0 = time.perf_counter()
+        for k in range(steps):
+            step(k)
+        for uu, _, _ in pipe:
+            native.check(lib.symgb_synchronize(uu.handle))
+        by_streams[cs] = max_over_ranks(world, (time.perf_counter() - t0) / steps)
+        barrier(world)
+    copy_streams = min(by_streams, key=by_streams.get)
+    t_e2e = by_streams[copy_streams]
     got = pipe[1][2].numpy().reshape(S, -1)
     err = max(err, max(rel_err(got[s], w.numeric, floor) for s in (0, S - 1)))
     u2.close()
@@ -521,6 +529,8 @@ def end_to_end(args, w, u, make_unit, apply, sched, inputs, nnz, S, floor, world
             "mode": "two units on two streams take alternate steps (async set_arg / run / get_result: results "
                     "gathered on the device and copied to page-locked memory on the unit's copy stream); every "
                     "step copies its inputs in and its results out; no L2 clearing",
+            "copy_streams": copy_streams,
+            "ms_per_step_by_copy_streams": {str(k): v * 1e3 for k, v in by_streams.items()},
             "one_at_a_time": {"value": world * nnz * S / t_seq, "ms_per_step": t_seq * 1e3}}
 
 

@@ -200,7 +200,7 @@ const char* symgb_last_error(void);
 int symgb_set_schedule(symgb_unit_t u, const symgb_schedule* s);
 int symgb_get_schedule(symgb_unit_t u, symgb_schedule* s);
 
-/* Number of value sets evaluated per run (default 1).  Reallocates x. */
+/* Number of value sets evaluated per run (1 .. 2^20, default 1).  Reallocates x. */
 int symgb_set_num_sets(symgb_unit_t u, int num_sets);
 int symgb_num_sets(symgb_unit_t u);
 
@@ -228,6 +228,12 @@ int symgb_synchronize(symgb_unit_t u);
  * both streams. */
 int symgb_set_arg_sets_async(symgb_unit_t u, const double* d, int i);
 int symgb_get_result_sets_async(symgb_unit_t u, double* d, int k);
+
+/* Copy streams of symgb_get_result_sets_async (1..8, default 1): a result of
+   n >= 8 MiB is split into min(count, n / 8 MiB) chunks, each copied on its
+   own stream (several copy engines); the completion the next call waits for
+   covers every chunk. */
+int symgb_set_copy_streams(symgb_unit_t u, int count);
 
 /* Batches of units (many patterns of uneven size): one evaluation of every
  * unit, each with its own schedule and value sets, captured into one CUDA graph

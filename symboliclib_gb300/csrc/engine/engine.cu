@@ -67,6 +67,54 @@ __global__ void scatterKernel(const double* __restrict__ in, std::uint64_t start
     x[(start + j) * S + s] = __ldg(in + (std::uint64_t)s * len + j);
 }
 
+// The same two copies for many value sets, through a 32 x 32 tile in shared
+// memory: one warp reads the 32 consecutive sets of one slot (256 contiguous
+// bytes of x) and writes 32 consecutive positions of one set, so both sides
+// are coalesced (the one-thread-per-value kernels above read 8 bytes per
+// 32-byte sector on one side).  Grid: (ceil(len / 32), ceil(S / 32)), 256
+// threads.
+constexpr unsigned kSetTile = 32;
+
+// out[s * len + j] = x[ids[j] * S + s]
+__global__ void __launch_bounds__(256) gatherSetsKernel(const double* __restrict__ x,
+                                                        const std::uint32_t* __restrict__ ids, std::uint64_t len,
+                                                        unsigned S, double* __restrict__ out) {
+    __shared__ double tile[kSetTile][kSetTile + 1];
+    const std::uint64_t j0 = (std::uint64_t)blockIdx.x * kSetTile;
+    const unsigned s0 = blockIdx.y * kSetTile;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (unsigned p = warp; p < kSetTile; p += 8) {
+        const std::uint64_t j = j0 + p;
+        if (j < len && s0 + lane < S) tile[p][lane] = __ldg(x + (std::uint64_t)__ldg(ids + j) * S + s0 + lane);
+    }
+    __syncthreads();
+    for (unsigned q = warp; q < kSetTile; q += 8) {
+        const std::uint64_t j = j0 + lane;
+        if (s0 + q < S && j < len) out[(std::uint64_t)(s0 + q) * len + j] = tile[lane][q];
+    }
+}
+
+// x[(start + j) * S + s] = in[s * len + j]
+__global__ void __launch_bounds__(256) scatterSetsKernel(const double* __restrict__ in, std::uint64_t start,
+                                                         std::uint64_t len, unsigned S, double* __restrict__ x) {
+    __shared__ double tile[kSetTile][kSetTile + 1];
+    const std::uint64_t j0 = (std::uint64_t)blockIdx.x * kSetTile;
+    const unsigned s0 = blockIdx.y * kSetTile;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (unsigned q = warp; q < kSetTile; q += 8) {
+        const std::uint64_t j = j0 + lane;
+        if (s0 + q < S && j < len) tile[lane][q] = __ldg(in + (std::uint64_t)(s0 + q) * len + j);
+    }
+    __syncthreads();
+    for (unsigned p = warp; p < kSetTile; p += 8) {
+        const std::uint64_t j = j0 + p;
+        if (j < len && s0 + lane < S) x[(start + j) * S + s0 + lane] = tile[p][lane];
+    }
+}
+
+// Value-set counts from which the tiled kernels are used.
+constexpr unsigned kTiledSets = 8;
+
 // ------------------------------------------------------------------ host side
 
 }  // namespace
@@ -642,7 +690,11 @@ int symgb_get_result_sets_device(symgb_unit_t u, double* d, int k) {
     if (k < 0 || (std::size_t)k >= u->outStart.size() || !d) return fail(SYMGB_ERR_ARGUMENT, "bad result index");
     const std::uint64_t len = u->outLength[k];
     const std::uint64_t work = len * u->numSets;
-    if (work) {
+    if (work && u->numSets >= kTiledSets) {
+        const dim3 grid((unsigned)((len + kSetTile - 1) / kSetTile), (unsigned)((u->numSets + kSetTile - 1) / kSetTile));
+        gatherSetsKernel<<<grid, 256, 0, u->stream>>>(u->x.ptr, u->ids.ptr + u->outStart[k], len, (unsigned)u->numSets, d);
+        SYMGB_CUDA(cudaGetLastError());
+    } else if (work) {
         gatherKernel<<<(unsigned)((work + 255) / 256), 256, 0, u->stream>>>(u->x.ptr, u->ids.ptr + u->outStart[k], len,
                                                                             (unsigned)u->numSets, d);
         SYMGB_CUDA(cudaGetLastError());
@@ -690,7 +742,11 @@ int symgb_set_arg_sets_device(symgb_unit_t u, const double* d, int i) {
         return SYMGB_OK;
     }
     const std::uint64_t work = len * u->numSets;
-    if (work) {
+    if (work && u->numSets >= kTiledSets) {
+        const dim3 grid((unsigned)((len + kSetTile - 1) / kSetTile), (unsigned)((u->numSets + kSetTile - 1) / kSetTile));
+        scatterSetsKernel<<<grid, 256, 0, u->stream>>>(d, u->argStart[i], len, (unsigned)u->numSets, u->x.ptr);
+        SYMGB_CUDA(cudaGetLastError());
+    } else if (work) {
         scatterKernel<<<(unsigned)((work + 255) / 256), 256, 0, u->stream>>>(d, u->argStart[i], len, (unsigned)u->numSets,
                                                                              u->x.ptr);
         SYMGB_CUDA(cudaGetLastError());
@@ -764,9 +820,35 @@ int symgb_get_result_sets_async(symgb_unit_t u, double* d, int k) {
     }
     if (int e = symgb_get_result_sets_device(u, buf, k)) return e;
     SYMGB_CUDA(cudaEventRecord(u->gatherDone, u->stream));
-    SYMGB_CUDA(cudaStreamWaitEvent(u->copyStream, u->gatherDone, 0));
-    SYMGB_CUDA(cudaMemcpyAsync(d, buf, n * 8, cudaMemcpyDeviceToHost, u->copyStream));
+    // Chunks of at least 8 MiB, one per copy stream in use.
+    const std::size_t minChunk = (8u << 20) / 8;
+    const std::size_t chunks = std::max<std::size_t>(1, std::min<std::size_t>((std::size_t)u->copyStreams, n / minChunk));
+    while (u->extraCopy.size() + 1 < chunks) {
+        cudaStream_t st;
+        cudaEvent_t ev;
+        SYMGB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        SYMGB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        u->extraCopy.push_back(st);
+        u->extraDone.push_back(ev);
+    }
+    const std::size_t per = (n + chunks - 1) / chunks;
+    for (std::size_t c = 0; c < chunks; ++c) {
+        cudaStream_t st = c == 0 ? u->copyStream : u->extraCopy[c - 1];
+        const std::size_t b0 = c * per, len = std::min(n, b0 + per) - std::min(n, b0);
+        SYMGB_CUDA(cudaStreamWaitEvent(st, u->gatherDone, 0));
+        if (len) SYMGB_CUDA(cudaMemcpyAsync(d + b0, buf + b0, len * 8, cudaMemcpyDeviceToHost, st));
+        if (c > 0) {
+            SYMGB_CUDA(cudaEventRecord(u->extraDone[c - 1], st));
+            SYMGB_CUDA(cudaStreamWaitEvent(u->copyStream, u->extraDone[c - 1], 0));
+        }
+    }
     SYMGB_CUDA(cudaEventRecord(u->copyDone[k], u->copyStream));
+    return SYMGB_OK;
+}
+
+int symgb_set_copy_streams(symgb_unit_t u, int n) {
+    if (!u || n < 1 || n > 8) return fail(SYMGB_ERR_ARGUMENT, "copy streams must be in [1, 8]");
+    u->copyStreams = n;
     return SYMGB_OK;
 }
 
@@ -913,7 +995,7 @@ int symgb_get_schedule(symgb_unit_t u, symgb_schedule* s) {
 }
 
 int symgb_set_num_sets(symgb_unit_t u, int num_sets) {
-    if (!u || num_sets < 1) return fail(SYMGB_ERR_ARGUMENT, "num_sets must be >= 1");
+    if (!u || num_sets < 1 || num_sets > (1 << 20)) return fail(SYMGB_ERR_ARGUMENT, "num_sets must be in [1, 2^20]");
     if (num_sets == u->numSets) return SYMGB_OK;
     u->numSets = num_sets;
     u->dropGraph();

@@ -81,6 +81,12 @@ struct symgb_unit {
     cudaStream_t copyStream = nullptr;
     cudaEvent_t gatherDone = nullptr;
     std::vector<cudaEvent_t> copyDone;
+    // Large result copies are split over copyStreams (symgb_set_copy_streams):
+    // copyStream and extraCopy[i], each chunk on its own stream so several
+    // copy engines move it; extraDone[i] joins chunk i + 1 back into copyStream.
+    int copyStreams = 1;
+    std::vector<cudaStream_t> extraCopy;
+    std::vector<cudaEvent_t> extraDone;
     DevBuf<double> asyncOut;
     int asyncOutSets = 0;
     DevBuf<std::uint32_t> p, ids;
@@ -127,6 +133,13 @@ struct symgb_unit {
         copyDone.clear();
         if (gatherDone) cudaEventDestroy(gatherDone);
         gatherDone = nullptr;
+        for (cudaStream_t e : extraCopy) {
+            cudaStreamSynchronize(e);
+            cudaStreamDestroy(e);
+        }
+        extraCopy.clear();
+        for (cudaEvent_t e : extraDone) cudaEventDestroy(e);
+        extraDone.clear();
         if (copyStream) cudaStreamDestroy(copyStream);
         copyStream = nullptr;
         asyncOut.reset();

@@ -112,6 +112,7 @@ SYMGB_FUNCTIONS = {
     "symgb_compiled_source": (C.c_int64, [C.c_void_p, C.c_int, C.c_char_p, C.c_uint64]),
     "symgb_compile_check": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "symgb_set_barrier_limits": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int]),
+    "symgb_set_copy_streams": (C.c_int, [C.c_void_p, C.c_int]),
     "symgb_kernel_program": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]),
 }
@@ -370,6 +371,10 @@ class Unit:
 
     def set_num_sets(self, n: int) -> None:
         check(self._lib.symgb_set_num_sets(self.handle, n))
+
+    def set_copy_streams(self, n: int) -> None:
+        """Streams the async result copy is split over (symgb_set_copy_streams)."""
+        check(self._lib.symgb_set_copy_streams(self.handle, n))
 
     @property
     def num_kernels(self) -> int:

@@ -86,6 +86,7 @@ def test_schedule_validation():
     native.check(lib.symgb_get_schedule(h, C.byref(got)))
     assert (got.kind, got.threads_per_block) == (2, 64)
     assert lib.symgb_set_num_sets(h, 0) == -1
+    assert lib.symgb_set_num_sets(h, (1 << 20) + 1) == -1
     native.check(lib.symgb_set_num_sets(h, 5))
     assert lib.symgb_num_sets(h) == 5
     lib.symgb_unit_destroy(h)

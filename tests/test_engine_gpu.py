@@ -71,7 +71,7 @@ def test_fast_mode_within_tolerance(name, size, seed, kind, executor):
 
 @pytest.mark.parametrize("name,size,seed", [("cotan", 8, 22), ("cloth", 5, 32), ("ata", 9, 12)])
 @pytest.mark.parametrize("kind", SCHEDULES)
-@pytest.mark.parametrize("sets", [2, 7, 33, 64])
+@pytest.mark.parametrize("sets", [2, 7, 8, 32, 33, 64])
 @pytest.mark.parametrize("executor", EXECUTORS)
 def test_value_set_batches_match_oracle(name, size, seed, kind, sets, executor):
     """S value sets in one run: every set bit-identical (exact mode) to the
@@ -149,7 +149,7 @@ def test_lanes_per_item(lanes, tpb):
         assert bits_equal(out[0], gold) and bits_equal(out[4], gold), name
 
 
-@pytest.mark.parametrize("sets", [1, 3])
+@pytest.mark.parametrize("sets", [1, 3, 40])
 def test_results_into_page_locked_memory(sets):
     """getResult into page-locked host memory (written by the gather kernel
     directly) equals getResult into ordinary memory."""
@@ -242,6 +242,36 @@ def test_async_results_of_consecutive_executes_stay_apart():
             for s in range(sets):
                 ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, per_set[s])[0]
                 assert bits_equal(got[s], ref), (sets, s)
+
+
+@pytest.mark.parametrize("copy_streams", [1, 3, 8])
+def test_async_result_copy_in_chunks(copy_streams):
+    """A 72 MiB result (cloth 60 x 60, 64 value sets) split over up to 8 copy
+    streams arrives whole: bit-identical to the synchronous result, twice in a
+    row (the second gather waits for every chunk of the first copy)."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    w = native.Workload("cloth", 60, 4)
+    lib = native.symgb()
+    sets = 64
+    u = native.Unit.from_workload(w)
+    u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_EXACT)
+    u.set_num_sets(sets)
+    u.set_copy_streams(copy_streams)
+    ins = [torch.from_numpy(np.tile(a, sets)).pin_memory() for a in w.inputs]
+    for i, a in enumerate(ins):
+        native.check(lib.symgb_set_arg_sets(u.handle, C.c_void_p(a.data_ptr()), i))
+    u.run()
+    ref = u.get_result(0)
+    assert len(ref) * 8 >= 8 * (8 << 20)
+    outs = [torch.full((len(ref),), -1.0, dtype=torch.float64).pin_memory() for _ in range(2)]
+    for o in outs:
+        native.check(lib.symgb_run_async(u.handle))
+        native.check(lib.symgb_get_result_sets_async(u.handle, C.c_void_p(o.data_ptr()), 0))
+    native.check(lib.symgb_synchronize(u.handle))
+    for o in outs:
+        assert bits_equal(o.numpy(), ref)
+    assert lib.symgb_set_copy_streams(u.handle, 0) == -1 and lib.symgb_set_copy_streams(u.handle, 9) == -1
 
 
 def test_larger_cases_match_oracle():
