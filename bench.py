@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--items", type=int, default=1, help="work items per thread (1, 2, 4)")
     ap.add_argument("--lanes", type=int, default=1, help="threads per work item (interpreter: 1, 2, 4, 8)")
     ap.add_argument("--tpb", type=int, default=128, help="threads per block")
+    ap.add_argument("--min-blocks", type=int, default=0,
+                    help="compiled executor: minimum resident CTAs per SM the kernels are compiled for (0: compiler)")
     ap.add_argument("--math", default="fast", choices=["fast", "exact"])
     ap.add_argument("--executor", default="compiled", choices=["compiled", "interpreter"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -139,9 +141,10 @@ class ClockSampler:
 # step's launches) and FP64 pipe utilisation per launch from ncu captures of
 # the compiled executor on a GB300, summarised (with their commands) in
 # profiles/.  Keyed by (workload, size, value sets, schedule kind, threads per
-# block, items per thread); configurations not captured report null.
+# block, items per thread, minimum CTAs per SM); configurations not captured
+# report null.
 MEASURED = {
-    ("cotan", 500, 1, "levels", 128, 1): {"traffic": 126.3e6, "fp64_pipe_busy": [0.818, 0.852, 0.416],
+    ("cotan", 500, 1, "levels", 128, 1, 0): {"traffic": 126.3e6, "fp64_pipe_busy": [0.818, 0.852, 0.416],
                                           "profile": "profiles/symgb_cotan500_levels.md"},
 }
 
@@ -266,8 +269,8 @@ def run_reference(args):
 
 # Candidates of the on-the-spot tuning (compiled executor): kind, threads per
 # block, items per thread.
-TUNE_SPACE = [("plain", 64, 4), ("plain", 128, 2), ("plain", 128, 4), ("levels", 64, 4), ("levels", 128, 1),
-              ("levels", 128, 2), ("levels", 256, 1), ("persistent", 128, 4)]
+TUNE_SPACE = [("plain", 64, 4, 0), ("plain", 128, 2, 0), ("plain", 128, 4, 0), ("levels", 64, 4, 0),
+              ("levels", 128, 1, 0), ("levels", 128, 2, 0), ("levels", 256, 1, 0), ("persistent", 128, 4, 0)]
 
 
 def fp64_instructions(u, tuner, math):
@@ -312,9 +315,9 @@ def main_engine(args):
         u.set_num_sets(S)
         return u, st
 
-    def apply(u, kind, tpb, items):
+    def apply(u, kind, tpb, items, minb):
         u.set_schedule(kind=kinds[kind], math=math, threads_per_block=tpb, items_per_thread=items,
-                       lanes_per_item=args.lanes, executor=execs[args.executor])
+                       lanes_per_item=args.lanes, executor=execs[args.executor], blocks_per_sm=minb)
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -347,12 +350,13 @@ def main_engine(args):
             compile_s += u.prepare()
             timings[cand] = float(np.median(time_runs(u, stream, 3)))
         best = min(timings, key=timings.get)
-        tuning = {"candidates_ms": {f"{k} tpb{t} items{i}": round(v, 4) for (k, t, i), v in timings.items()},
+        tuning = {"candidates_ms": {f"{k} tpb{t} items{i}" + (f" minblocks{m}" if m else ""): round(v, 4)
+                                    for (k, t, i, m), v in timings.items()},
                   "seconds": round(time.perf_counter() - t_tune, 1)}
-        kind, tpb, items = best
+        kind, tpb, items, minb = best
     else:
-        kind, tpb, items = args.schedule, args.tpb, args.items
-    apply(u, kind, tpb, items)
+        kind, tpb, items, minb = args.schedule, args.tpb, args.items, args.min_blocks
+    apply(u, kind, tpb, items, minb)
     compile_s += u.prepare()
     u.run()
     out = u.get_result(0).reshape(S, -1)
@@ -400,8 +404,8 @@ def main_engine(args):
     # end to end through the C ABI with page-locked host buffers
     e2e = None
     if not args.no_e2e:
-        e2e = end_to_end(args, w, u, make_unit, apply, (kind, tpb, items), inputs, nnz, S, floor, world, lib, native,
-                         torch)
+        e2e = end_to_end(args, w, u, make_unit, apply, (kind, tpb, items, minb), inputs, nnz, S, floor, world, lib,
+                         native, torch)
 
     stats = u.stats()
     alg_bytes = u.algorithmic_bytes(S)
@@ -413,13 +417,14 @@ def main_engine(args):
     flops_w = (stats.flops + 10 * stats.divs + 10 * stats.sqrts) * S
     from symboliclib_gb300 import tuner
     fp64_instr = fp64_instructions(u, tuner, math) * S
-    meas = MEASURED.get((args.workload, args.size, S, kind, tpb, items), {})
+    meas = MEASURED.get((args.workload, args.size, S, kind, tpb, items, minb), {})
 
     if rank != 0:
         return
     cfg = {"workload": workload_name(args), "size": args.size, "output_nnz": nnz, "value_sets": S,
            "seed": args.seed, "inputs": "the seeded state, the same in every value set",
            "schedule": kind, "executor": args.executor, "threads_per_block": tpb, "items_per_thread": items,
+           "min_blocks_per_sm": minb,
            "math": args.math, "tuning": tuning, "compile_s": round(compile_s, 2),
            "l2": "cleared before every step (256 MiB write)",
            "front_end_s": round(front_s, 1), "model_s": round(w.model_seconds, 1),

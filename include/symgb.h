@@ -102,9 +102,12 @@ typedef struct symgb_schedule {
     int32_t math;               /* SYMGB_MATH_* */
     int32_t threads_per_block;  /* 0 = plan default */
     int32_t items_per_tile;     /* work items per CTA tile in fused schedules (0 = auto) */
-    int32_t blocks_per_sm;      /* CTAs per SM.  Persistent: 0 = occupancy maximum.  Plain and
-                                   levels: 0 = one CTA per tile, > 0 caps the grid at this many
-                                   CTAs per SM, each taking several tiles */
+    int32_t blocks_per_sm;      /* CTAs per SM.  Interpreter, persistent: 0 = occupancy maximum;
+                                   plain and levels: 0 = one CTA per tile, > 0 caps the grid at
+                                   this many CTAs per SM, each taking several tiles.  Compiled
+                                   executor: > 0 is the minimum of resident CTAs per SM its
+                                   kernels are compiled for (__launch_bounds__), which caps their
+                                   registers; 0 = the compiler's choice */
     int32_t use_graph;          /* capture run() into a CUDA graph and replay it */
     int32_t items_per_thread;   /* work items per thread per pass: 1, 2 or 4 (0 = 1) */
     int32_t fusion_depth;       /* LEVELS: consecutive levels per launch (0/1 = one level; a
@@ -122,8 +125,9 @@ typedef struct symgb_schedule {
  *     per thread, compiled for sm_103a by NVRTC at the first run of a
  *     configuration (math mode, value sets, schedule, block sizes) and cached
  *     for the process; consecutive launches overlap their start-up
- *     (programmatic dependent launch).  items_per_thread, lanes_per_item,
- *     items_per_tile and fusion_depth do not apply.
+ *     (programmatic dependent launch).  A thread takes items_per_thread work
+ *     items (1, 2 or 4, unrolled); lanes_per_item, items_per_tile and
+ *     fusion_depth do not apply.
  *   INTERPRETER: one precompiled kernel runs every template as a bundled
  *     register-machine program (no run-time compilation). */
 #define SYMGB_EXEC_COMPILED 0
@@ -145,6 +149,11 @@ int symgb_prepare(symgb_unit_t u, double* compile_seconds);
  * failure) and reports the compile time. */
 int64_t symgb_compiled_source(symgb_unit_t u, int kind, char* buf, uint64_t cap);
 int symgb_compile_check(symgb_unit_t u, int kind, double* seconds);
+
+/* Registers per thread of each launch of the compiled module of schedule
+ * `kind` (compiled and loaded if needed; needs an initialised unit): writes up
+ * to `cap` entries in launch order and returns the number of launches. */
+int symgb_compiled_registers(symgb_unit_t u, int kind, int* registers, int cap);
 
 /* Failure-handling tests only: the limit of every bounded grid-barrier wait
  * (default 2 s) and a number of arrivals each barrier waits for beyond the

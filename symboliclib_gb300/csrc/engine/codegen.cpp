@@ -203,6 +203,19 @@ int checkedItems(int items) {
 
 extern const char* const kJitPrelude;
 
+namespace {
+
+// `__launch_bounds__(tpb)` or, with a minimum CTA count per SM that fits the
+// SM's 2048 threads, `__launch_bounds__(tpb, minBlocks)`.
+std::string launchBounds(int tpb, int minBlocks) {
+    std::string s = "__launch_bounds__(" + std::to_string(tpb);
+    const int fit = std::min(minBlocks, 2048 / std::max(1, tpb));
+    if (fit > 0) s += ", " + std::to_string(fit);
+    return s + ")";
+}
+
+}  // namespace
+
 JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLevels, const JitConfig& cfg) {
     JitSource out;
     std::ostringstream os;
@@ -231,7 +244,7 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
             const int tpb = cfg.kernelTpb.at(k);
             const int items = checkedItems(cfg.kernelItems.at(k));
             const std::string name = "symgb_k" + std::to_string(k);
-            os << "extern \"C\" __global__ void __launch_bounds__(" << tpb << ") " << name << params << ") {\n"
+            os << "extern \"C\" __global__ void " << launchBounds(tpb, cfg.minBlocks) << " " << name << params << ") {\n"
                << "    symgbDependencyWait();\n    symgbLaunchDependents();\n";
             emitItems(os, (int)k, total, S, tpb, items, 0, "(unsigned long long)blockIdx.x", "    ");
             os << "}\n\n";
@@ -247,7 +260,7 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
             const int tpb = cfg.levelTpb.at(L);
             const int items = checkedItems(cfg.levelItems.at(L));
             const std::string name = "symgb_l" + std::to_string(L);
-            os << "extern \"C\" __global__ void __launch_bounds__(" << tpb << ") " << name << params << ") {\n"
+            os << "extern \"C\" __global__ void " << launchBounds(tpb, cfg.minBlocks) << " " << name << params << ") {\n"
                << "    symgbDependencyWait();\n    symgbLaunchDependents();\n"
                << "    const unsigned long long b = blockIdx.x;\n";
             emitDispatch(os, ks, descs, S, tpb, items, 0, "    ");
@@ -258,7 +271,7 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
         const int tpb = cfg.levelTpb.at(0);
         const int items = checkedItems(cfg.levelItems.at(0));
         os << "struct SymgbBarrier { unsigned count; unsigned generation; int error; int pad; };\n";
-        os << "extern \"C\" __global__ void __launch_bounds__(" << tpb << ") symgb_persistent" << params
+        os << "extern \"C\" __global__ void " << launchBounds(tpb, cfg.minBlocks) << " symgb_persistent" << params
            << ", SymgbBarrier* bar, int* hostError, unsigned long long timeoutNs, unsigned extra) {\n"
            << "    symgbDependencyWait();\n";
         std::uint64_t most = 1;

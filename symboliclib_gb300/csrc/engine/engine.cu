@@ -253,6 +253,7 @@ JitConfig jitConfig(const symgb_unit* u, int kind) {
     c.kind = kind == SYMGB_SCHEDULE_PLAIN ? JIT_PLAIN : kind == SYMGB_SCHEDULE_LEVELS ? JIT_LEVELS : JIT_PERSISTENT;
     c.math = u->sched.math;
     c.numSets = (unsigned)u->numSets;
+    c.minBlocks = std::max(0, u->sched.blocks_per_sm);
     for (std::size_t k = 0; k < u->kernels.size(); ++k) {
         c.kernelTpb.push_back(u->shapeOf(k).tpb);
         c.kernelItems.push_back(u->shapeOf(k).items);
@@ -286,6 +287,7 @@ std::string jitKeyOf(const JitConfig& c) {
     for (int t : c.kernelItems) k += std::to_string(t) + ",";
     k += "/";
     for (int t : c.levelItems) k += std::to_string(t) + ",";
+    k += "/" + std::to_string(c.minBlocks);
     return k;
 }
 
@@ -945,6 +947,15 @@ int symgb_compile_check(symgb_unit_t u, int kind, double* seconds) {
     }
     if (int e = compileOnly(src, seconds, &err)) return fail(e, err);
     return SYMGB_OK;
+}
+
+int symgb_compiled_registers(symgb_unit_t u, int kind, int* registers, int cap) {
+    if (!u || kind < 0 || kind > 2 || cap < 0 || (cap > 0 && !registers)) return fail(SYMGB_ERR_ARGUMENT, "bad argument");
+    if (!u->initialized) return fail(SYMGB_ERR_STATE, "compiled_registers before init");
+    std::shared_ptr<const JitModule> m;
+    if (int e = getModule(u, kind, &m)) return e;
+    for (int i = 0; i < cap && i < (int)m->registers.size(); ++i) registers[i] = m->registers[i];
+    return (int)m->registers.size();
 }
 
 int symgb_set_barrier_limits(symgb_unit_t u, uint64_t timeout_ns, int extra_arrivals) {

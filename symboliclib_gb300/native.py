@@ -113,6 +113,7 @@ SYMGB_FUNCTIONS = {
     "symgb_compile_check": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "symgb_set_barrier_limits": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int]),
     "symgb_set_copy_streams": (C.c_int, [C.c_void_p, C.c_int]),
+    "symgb_compiled_registers": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "symgb_kernel_program": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]),
 }
@@ -371,6 +372,17 @@ class Unit:
 
     def set_num_sets(self, n: int) -> None:
         check(self._lib.symgb_set_num_sets(self.handle, n))
+
+    def compiled_registers(self, kind: int) -> list[int]:
+        """Registers per thread of every launch of the compiled module of `kind`."""
+        n = self._lib.symgb_compiled_registers(self.handle, kind, None, 0)
+        if n < 0:
+            check(n)
+        regs = (C.c_int * max(1, n))()
+        got = self._lib.symgb_compiled_registers(self.handle, kind, regs, n)
+        if got < 0:
+            check(got)
+        return list(regs)[:n]
 
     def set_copy_streams(self, n: int) -> None:
         """Streams the async result copy is split over (symgb_set_copy_streams)."""

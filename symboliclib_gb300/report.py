@@ -124,6 +124,13 @@ def single(args):
         "hbm_peak_gbs": peak, "fp64_peak_tflops": fp / 1e12}), flush=True)
 
 
+# Schedules the batch's autotuning chooses from (compiled executor): the
+# plain and levels shapes that win on cloth patterns from 16 x 16 to 300 x 300
+# with 1 to 64 value sets.
+BATCH_CANDIDATES = [tuner.Sched("plain", 4, 64, 1, 1, "compiled"), tuner.Sched("plain", 2, 128, 1, 1, "compiled"),
+                    tuner.Sched("levels", 1, 128, 1, 1, "compiled"), tuner.Sched("levels", 4, 64, 1, 1, "compiled")]
+
+
 def batch(args):
     import torch
     lib = native.symgb()
@@ -154,12 +161,22 @@ def batch(args):
             plain_by_side[key] = tuner.time_schedule(u, tuner.Sched("plain", 1, 128, 1, 1, "compiled"), stream, None,
                                                      runs=5) * 1e-6
         plain_s += plain_by_side[key] * S
-    # batched: each unit with its sets, tuned schedule choice per unit size class, one graph
+    # batched: each unit with its sets; with --schedule tuned the autotuner
+    # times BATCH_CANDIDATES on the first unit of every pattern (with that
+    # unit's sets) and the pattern's other units take its choice; one graph
+    chosen, t_tune = {}, time.perf_counter()
     for u, S, w in units:
         u.set_num_sets(S)
         for i, a in enumerate(w.inputs):
             u.set_arg(i, np.tile(a, S))
-        tuner.Sched(args.schedule, args.items, args.tpb, 1, args.lanes, args.executor).apply(u, graph=0)
+        if args.schedule == "tuned":
+            if w.size not in chosen:
+                ts = {c: tuner.time_schedule(u, c, stream, flush, runs=3) for c in BATCH_CANDIDATES}
+                chosen[w.size] = min(ts, key=ts.get)
+            chosen[w.size].apply(u, graph=0)
+        else:
+            tuner.Sched(args.schedule, args.items, args.tpb, 1, args.lanes, args.executor).apply(u, graph=0)
+    tune_s = time.perf_counter() - t_tune
     handles = (C.c_void_p * len(units))(*[u.handle.value for u, _, _ in units])
     b = C.c_void_p()
     t_create = time.perf_counter()
@@ -188,9 +205,11 @@ def batch(args):
         "instances": int(args.count), "sides": [int(sides.min()), int(sides.max())], "distinct_patterns": len(cache),
         "value_sets_total": int(sets.sum()), "output_nnz_total": int(total_nnz), "front_end_s": round(front, 1),
         "graph": {"ms": t_graph * 1e3, "nnz_per_s": total_nnz / t_graph, "kernels": int(launches),
-                  "streams": args.streams, "schedule": f"{args.executor} {args.schedule} items {args.items} "
-                                                        f"lanes {args.lanes} tpb {args.tpb}",
-                  "create_s": round(create_s, 1)},
+                  "streams": args.streams, "create_s": round(create_s, 1),
+                  "schedule": ({str(c): sum(1 for v in chosen.values() if v == c) for c in BATCH_CANDIDATES}
+                               if args.schedule == "tuned" else
+                               f"{args.executor} {args.schedule} items {args.items} lanes {args.lanes} tpb {args.tpb}"),
+                  "tuning_s": round(tune_s, 1)},
         "plain_per_call": {"ms": plain_s * 1e3, "nnz_per_s": total_nnz / plain_s},
         "speedup": plain_s / t_graph, "max_rel_err_sampled": max(errs)}), flush=True)
 
@@ -391,7 +410,7 @@ def main():
     b.add_argument("--max-side", type=int, default=48)
     b.add_argument("--max-sets", type=int, default=16)
     b.add_argument("--streams", type=int, default=8)
-    b.add_argument("--schedule", default="levels", choices=list(tuner.KINDS))
+    b.add_argument("--schedule", default="tuned", choices=["tuned"] + list(tuner.KINDS))
     b.add_argument("--items", type=int, default=1)
     b.add_argument("--lanes", type=int, default=1)
     b.add_argument("--executor", default="compiled", choices=["compiled", "interpreter"])

@@ -196,3 +196,18 @@ def test_items_per_thread_cover_every_work_item():
         assert f"* {96 * items}ull + threadIdx.x" in src
         if items > 1:
             assert f"for (int j = 0; j < {items}; ++j)" in src
+
+
+def test_minimum_blocks_per_sm_become_launch_bounds():
+    """blocks_per_sm > 0 compiles every entry point for that many resident
+    CTAs per SM (capped at the SM's 2048 threads); the module still compiles."""
+    w = native.Workload("cloth", 5, 32)
+    u = native.Unit.from_workload(w, init=False)
+    u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_FAST, threads_per_block=128, blocks_per_sm=6)
+    src = u.compiled_source(native.SCHEDULE_PLAIN)
+    assert "__launch_bounds__(128, 6)" in src and "__launch_bounds__(128)" not in src
+    assert u.compile_check(native.SCHEDULE_PLAIN) >= 0.0
+    u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_FAST, threads_per_block=512, blocks_per_sm=6)
+    assert "__launch_bounds__(512, 4)" in u.compiled_source(native.SCHEDULE_LEVELS)
+    u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_FAST, threads_per_block=128)
+    assert "__launch_bounds__(128)" in u.compiled_source(native.SCHEDULE_PLAIN)

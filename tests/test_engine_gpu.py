@@ -290,17 +290,19 @@ def test_larger_cases_match_oracle():
                 assert bits_equal(u.get_result(0), ref), (name, kind, executor)
 
 
-@pytest.mark.parametrize("tpb,items", [(32, 1), (96, 2), (128, 4), (256, 1), (512, 2)])
+@pytest.mark.parametrize("tpb,items,minb", [(32, 1, 0), (96, 2, 0), (128, 4, 0), (256, 1, 0), (512, 2, 0),
+                                            (64, 4, 6), (128, 2, 8)])
 @pytest.mark.parametrize("kind", SCHEDULES)
-def test_compiled_block_sizes(tpb, items, kind):
-    """The compiled executor at several block sizes and work items per thread
-    (partial last blocks, level dispatch boundaries) and 1 or 5 value sets:
-    bit-identical."""
+def test_compiled_block_sizes(tpb, items, minb, kind):
+    """The compiled executor at several block sizes, work items per thread and
+    register caps (minimum resident CTAs per SM), with partial last blocks,
+    level dispatch boundaries and 1 or 5 value sets: bit-identical."""
     for name, size, seed in [("cotan", 8, 22), ("cloth", 5, 32), ("neohookean", 1, 41)]:
         _, inp, gold = load_golden(name, size)
         w = native.Workload(name, size, seed)
         u = native.Unit.from_workload(w)
-        u.set_schedule(kind=kind, math=native.MATH_EXACT, threads_per_block=tpb, items_per_thread=items)
+        u.set_schedule(kind=kind, math=native.MATH_EXACT, threads_per_block=tpb, items_per_thread=items,
+                       blocks_per_sm=minb)
         for sets in (1, 5):
             u.set_num_sets(sets)
             for i, a in enumerate(split_inputs(w, inp)):
