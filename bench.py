@@ -144,8 +144,13 @@ class ClockSampler:
 # block, items per thread, minimum CTAs per SM); configurations not captured
 # report null.
 MEASURED = {
-    ("cotan", 500, 1, "levels", 128, 1, 0): {"traffic": 126.3e6, "fp64_pipe_busy": [0.818, 0.852, 0.416],
-                                          "profile": "profiles/symgb_cotan500_levels.md"},
+    ("cotan", 500, 1, "levels", 128, 1, 0): {"traffic": 81.77e6, "fp64_pipe_busy": [0.819, 0.851, 0.411],
+                                             "profile": "profiles/symgb_cotan500_levels.md"},
+    # symgb_k1 (the face-block template) at full size: one single-pass capture
+    # (dram__bytes_read.sum 389.07 MB + dram__bytes_write.sum 8.18 GB); its
+    # FP64 pipe share from the full section set on cloth 100 x 100 x 16 sets
+    ("cloth", 300, 64, "plain", 64, 4, 0): {"kernel_traffic": 8.569e9, "kernel_fp64_pipe_busy": 0.853,
+                                            "profile": "profiles/symgb_cloth100_k1.md"},
 }
 
 
@@ -387,6 +392,12 @@ def main_engine(args):
     t_step = max_over_ranks(world, float(np.mean(step_ms)) * 1e-3)
     value = world * nnz * S / t_step
 
+    # dominant kernel: every kernel timed with CUDA events on the unit's
+    # stream over as many steps as the timed region (plain launches of the
+    # chosen shape, L2 cleared before every step)
+    us_k = u.time_kernels(reps=args.steps, flush=flush)
+    kd = int(np.argmax(us_k))
+
     # plain per-call path: one value set per execute, one launch per kernel
     up = native.Unit.from_workload(w)
     stp = torch.cuda.Stream()
@@ -418,6 +429,15 @@ def main_engine(args):
     from symboliclib_gb300 import tuner
     fp64_instr = fp64_instructions(u, tuner, math) * S
     meas = MEASURED.get((args.workload, args.size, S, kind, tpb, items, minb), {})
+    # the dominant kernel's algorithmic bytes per launch: every gathered value
+    # and every result once per value set, its index and constant rows once
+    kdesc = w.plan.contents.kernels[kd]
+    ksum = tuner.program_summary(u, kd, math)
+    n_k = int(kdesc.num_instances)
+    k_bytes = S * 8 * n_k * (ksum["ldx"] + ksum["st"]) + 8 * n_k * ksum["ldc"] + 4 * n_k * int(kdesc.num_index_rows)
+    k_fp64 = (ksum["add"] + ksum["sub"] + ksum["mul"] + ksum["fma"] + 5 * ksum["div"] + 6 * ksum["sqrt"] +
+              4 * ksum["rec"]) * n_k * S
+    t_k = us_k[kd] * 1e-6
 
     if rank != 0:
         return
@@ -440,10 +460,23 @@ def main_engine(args):
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh)", "config": cfg,
             "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": meas.get("traffic"), "traffic_unit": "DRAM bytes per step (ncu capture)",
-                         "algorithmic_bytes_per_step": alg_bytes},
+            "roofline": {"bound": "hbm", "kernel": f"symgb_k{kd}", "achieved": k_bytes / t_k / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": k_bytes / t_k / 1e9 / peak, "peak_source": peak_kind,
+                         "traffic": meas.get("kernel_traffic"),
+                         "traffic_unit": "DRAM bytes per launch of the kernel (ncu capture)",
+                         "algorithmic_bytes_per_launch": k_bytes, "ms_per_launch": t_k * 1e3,
+                         "launches_per_step": 1, "share_of_step": t_k / t_step,
+                         "fp64_instructions_per_launch": k_fp64,
+                         "fp64_pipe_frac": k_fp64 / t_k / (fp64.value / 2),
+                         "fp64_pipe_busy_ncu": meas.get("kernel_fp64_pipe_busy"),
+                         "timing": "CUDA events around every kernel on the unit's stream, plain launches of the "
+                                   "chosen shape, as many steps as the timed region, L2 cleared before each",
+                         "bytes_note": "every gathered value and every result once per value set, index and "
+                                       "constant rows once"},
+            "roofline_step": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                              "frac": achieved / peak, "peak_source": peak_kind,
+                              "traffic": meas.get("traffic"), "traffic_unit": "DRAM bytes per step (ncu capture)",
+                              "algorithmic_bytes_per_step": alg_bytes},
             "fp64": {"flops_per_step_weighted": flops_w, "achieved_tflops": flops_w / t_step / 1e12,
                      "peak_tflops": fp64.value / 1e12,
                      "peak_source": "nominal" if args.no_fp64_probe else "measured",

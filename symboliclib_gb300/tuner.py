@@ -212,7 +212,10 @@ def program_summary(unit: native.Unit, k: int, math_mode: int = native.MATH_FAST
         bundles += 1
         entries += cnt
         pc += 1 + (cnt + 1) // 2
-    return {"registers": r.value, "loads": nl.value, "bundles": bundles, "entries": entries, **counts}
+    ldx = sum(1 for w in words[:nl.value] if w & 0xff == 1)  # x gathers (OP_LDX)
+    ldc = sum(1 for w in words[:nl.value] if w & 0xff == 2)  # constant-table reads (OP_LDC)
+    return {"registers": r.value, "loads": nl.value, "ldx": ldx, "ldc": ldc, "bundles": bundles, "entries": entries,
+            **counts}
 
 
 def kernel_features(unit: native.Unit, k: int, num_sets: int, shape, summary: dict) -> np.ndarray:
