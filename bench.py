@@ -146,11 +146,14 @@ class ClockSampler:
 MEASURED = {
     ("cotan", 500, 1, "levels", 128, 1, 0): {"traffic": 81.77e6, "fp64_pipe_busy": [0.819, 0.851, 0.411],
                                              "profile": "profiles/symgb_cotan500_levels.md"},
-    # symgb_k1 (the face-block template) at full size: one single-pass capture
-    # (dram__bytes_read.sum 389.07 MB + dram__bytes_write.sum 8.18 GB); its
-    # FP64 pipe share from the full section set on cloth 100 x 100 x 16 sets
+    # full size, single-pass captures: symgb_k1 (the face-block template)
+    # 389.07 MB read + 8.18 GB written per launch; the step's 18 kernels
+    # 18.707 GB; k1's FP64 pipe share from the full section set on cloth
+    # 100 x 100 x 16 sets
     ("cloth", 300, 64, "plain", 64, 4, 0): {"kernel_traffic": 8.569e9, "kernel_fp64_pipe_busy": 0.853,
-                                            "profile": "profiles/symgb_cloth100_k1.md"},
+                                            "traffic": 18.707e9,
+                                            "profile": "profiles/symgb_cloth100_k1.md, "
+                                                       "profiles/traffic_cloth300x64_plain.md"},
 }
 
 

@@ -8,10 +8,11 @@
 #define SYMGB_ERR_TIMEOUT (-4)
 #endif
 
-// Negation flips the sign bit (as C's unary minus does), on the integer pipe.
-__device__ __forceinline__ double symgbNegate(double x) {
-    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
-}
+// Negation flips the sign (C's unary minus; exact, -(+0) = -0).  Written as
+// the language's negation so the compiler can fold it into the sign modifier
+// of the FMA, add or multiply that consumes it: no instruction of its own and
+// no step in the dependency chain.
+__device__ __forceinline__ double symgbNegate(double x) { return -x; }
 
 // Fast-mode division, reciprocal and square root (OP_FDIV, OP_FREC, OP_FSQRT;
 // exact mode keeps the IEEE operations).  Each starts from the hardware's
