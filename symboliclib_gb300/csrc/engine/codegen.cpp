@@ -50,8 +50,9 @@ const char* libName(int op) {
 
 // Emits the device function evaluating kernel k for one work item
 // (instance i, value set s).  L2 = 1 reads x through L2 only (values written
-// earlier in the same launch, persistent schedule).
-void emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, int math, unsigned S) {
+// earlier in the same launch, persistent schedule).  Returns the number of
+// operations of the template.
+std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, int math, unsigned S) {
     std::vector<std::uint64_t> loads;
     const std::vector<LinOp> ops = linearCode(d, math, &loads);
     const std::uint64_t n = d.num_instances;
@@ -147,22 +148,42 @@ void emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, int mat
         os << "    const double " << v << " = " << rhs << ";\n";
     }
     os << "}\n\n";
+    return ops.size();
 }
+
+// Templates of at most this many operations per thread (operations x items)
+// get a second, unguarded copy of the items loop for threads whose items are
+// all in range: without a bounds check per item the compiler can issue every
+// item's index and gather loads before the first item's arithmetic, which is
+// what a light, memory-bound template needs.  Heavier templates keep one
+// guarded loop (their loads are hidden by arithmetic, and the copy would
+// double their compile time).
+constexpr std::size_t kSplitOps = 1024;
 
 // Work items of kernel k for block `b0` (relative to the kernel's first
 // block): `items` per thread, consecutive threads on consecutive items in
 // each of the thread's rounds (coalesced), rounds unrolled so the items'
-// loads are in flight together.
+// loads are in flight together.  `split`: threads whose items are all in
+// range take an unguarded copy of the loop (kSplitOps).
 void emitItems(std::ostringstream& os, int k, std::uint64_t total, unsigned S, int tpb, int items, int l2,
-               const std::string& b0, const char* indent) {
+               const std::string& b0, const char* indent, bool split) {
     os << indent << "const unsigned long long w0 = (" << b0 << ") * " << (std::uint64_t)tpb * items
        << "ull + threadIdx.x;\n";
+    if (items > 1 && split) {
+        os << indent << "if (w0 + " << u64((std::uint64_t)(items - 1) * tpb) << " < " << u64(total) << ") {\n"
+           << indent << "    #pragma unroll\n" << indent << "    for (int j = 0; j < " << items << "; ++j) {\n"
+           << indent << "        const unsigned long long w = w0 + (unsigned long long)j * " << tpb << "ull;\n"
+           << indent << "        symgbBody" << k << "<" << l2 << ">(x, xw, p, c, w / " << S << "ull, (unsigned)(w % "
+           << S << "ull));\n"
+           << indent << "    }\n" << indent << "} else {\n";
+    }
     if (items > 1) os << indent << "#pragma unroll\n" << indent << "for (int j = 0; j < " << items << "; ++j) {\n";
     else os << indent << "{\n" << indent << "    const int j = 0;\n";
     os << indent << "    const unsigned long long w = w0 + (unsigned long long)j * " << tpb << "ull;\n"
        << indent << "    if (w < " << u64(total) << ") symgbBody" << k << "<" << l2 << ">(x, xw, p, c, w / " << S
        << "ull, (unsigned)(w % " << S << "ull));\n"
        << indent << "}\n";
+    if (items > 1 && split) os << indent << "}\n";
 }
 
 std::uint64_t blocksFor(std::uint64_t total, int tpb, int items) {
@@ -173,7 +194,7 @@ std::uint64_t blocksFor(std::uint64_t total, int tpb, int items) {
 // Dispatch of block `b` over the kernels of one launch (kernel-major block
 // ranges, each kernel's work items in consecutive blocks).
 void emitDispatch(std::ostringstream& os, const std::vector<int>& ks, const std::vector<symgb_kernel_desc>& descs,
-                  unsigned S, int tpb, int items, int l2, const char* indent) {
+                  const std::vector<std::size_t>& opCount, unsigned S, int tpb, int items, int l2, const char* indent) {
     std::uint64_t first = 0;
     const std::string inner = std::string(indent) + "    ";
     for (std::size_t q = 0; q < ks.size(); ++q) {
@@ -181,7 +202,8 @@ void emitDispatch(std::ostringstream& os, const std::vector<int>& ks, const std:
         const std::uint64_t total = descs[k].num_instances * S;
         const std::uint64_t blocks = blocksFor(total, tpb, items);
         os << indent << (q ? "else " : "") << "if (b < " << u64(first + blocks) << ") {\n";
-        emitItems(os, k, total, S, tpb, items, l2, "b - " + u64(first), inner.c_str());
+        emitItems(os, k, total, S, tpb, items, l2, "b - " + u64(first), inner.c_str(),
+                  opCount[k] * (std::size_t)items <= kSplitOps);
         os << indent << "}\n";
         first += blocks;
     }
@@ -227,7 +249,8 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
     os << kJitPrelude << "\n";
     os << "template <int L2>\n__device__ __forceinline__ double symgbLoadX(const double* a) {\n"
           "    return L2 ? __ldcg(a) : __ldg(a);\n}\n\n";
-    for (std::size_t k = 0; k < descs.size(); ++k) emitBody(os, (int)k, descs[k], cfg.math, S);
+    std::vector<std::size_t> opCount(descs.size());
+    for (std::size_t k = 0; k < descs.size(); ++k) opCount[k] = emitBody(os, (int)k, descs[k], cfg.math, S);
     const char* params = "(const double* SYMGB_XR x, double* SYMGB_XR xw, const unsigned* __restrict__ p, "
                          "const double* __restrict__ c";
     // Kernels of each level, heaviest first (their blocks are dispatched first).
@@ -246,7 +269,8 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
             const std::string name = "symgb_k" + std::to_string(k);
             os << "extern \"C\" __global__ void " << launchBounds(tpb, cfg.minBlocks) << " " << name << params << ") {\n"
                << "    symgbDependencyWait();\n    symgbLaunchDependents();\n";
-            emitItems(os, (int)k, total, S, tpb, items, 0, "(unsigned long long)blockIdx.x", "    ");
+            emitItems(os, (int)k, total, S, tpb, items, 0, "(unsigned long long)blockIdx.x", "    ",
+                      opCount[k] * (std::size_t)items <= kSplitOps);
             os << "}\n\n";
             out.launches.push_back({name, (int)k, -1, blocksFor(total, tpb, items), tpb, items, false});
         }
@@ -263,7 +287,7 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
             os << "extern \"C\" __global__ void " << launchBounds(tpb, cfg.minBlocks) << " " << name << params << ") {\n"
                << "    symgbDependencyWait();\n    symgbLaunchDependents();\n"
                << "    const unsigned long long b = blockIdx.x;\n";
-            emitDispatch(os, ks, descs, S, tpb, items, 0, "    ");
+            emitDispatch(os, ks, descs, opCount, S, tpb, items, 0, "    ");
             os << "}\n\n";
             out.launches.push_back({name, -1, L, blocksOf(ks, descs, S, tpb, items), tpb, items, false});
         }
@@ -284,7 +308,7 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
             const std::uint64_t nb = blocksOf(ks, descs, S, tpb, items);
             most = std::max(most, nb);
             os << "    for (unsigned long long b = blockIdx.x; b < " << u64(nb) << "; b += gridDim.x) {\n";
-            emitDispatch(os, ks, descs, S, tpb, items, firstLevel ? 0 : 1, "        ");
+            emitDispatch(os, ks, descs, opCount, S, tpb, items, firstLevel ? 0 : 1, "        ");
             os << "    }\n";
             firstLevel = false;
         }

@@ -211,3 +211,24 @@ def test_minimum_blocks_per_sm_become_launch_bounds():
     assert "__launch_bounds__(512, 4)" in u.compiled_source(native.SCHEDULE_LEVELS)
     u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_FAST, threads_per_block=128)
     assert "__launch_bounds__(128)" in u.compiled_source(native.SCHEDULE_PLAIN)
+
+
+def test_light_templates_get_an_unguarded_items_loop():
+    """With several items per thread, a light template's threads whose items
+    are all in range run them without per-item bounds checks (so their loads
+    can be issued together); heavy templates keep the guarded loop only."""
+    w = native.Workload("cloth", 5, 32)
+    u = native.Unit.from_workload(w, init=False)
+    u.set_schedule(kind=native.SCHEDULE_PLAIN, math=native.MATH_FAST, threads_per_block=64, items_per_thread=4)
+    u.set_num_sets(8)
+    src = u.compiled_source(native.SCHEDULE_PLAIN)
+    kernels = {m.group(1): src[m.start():src.index("\n}\n", m.start())]
+               for m in re.finditer(r'void __launch_bounds__\(64\) (symgb_k\d+)', src)}
+    light = [k for k, body in kernels.items() if "} else {" in body]
+    heavy = [k for k, body in kernels.items() if "} else {" not in body]
+    assert light and heavy
+    for k in light:
+        body = kernels[k]
+        assert "if (w0 + 192ull < " in body
+    assert u.compile_check(native.SCHEDULE_PLAIN) >= 0.0
+    assert u.compile_check(native.SCHEDULE_PERSISTENT) >= 0.0
