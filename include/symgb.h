@@ -155,6 +155,15 @@ int symgb_compile_check(symgb_unit_t u, int kind, double* seconds);
  * to `cap` entries in launch order and returns the number of launches. */
 int symgb_compiled_registers(symgb_unit_t u, int kind, int* registers, int cap);
 
+/* Data path of the compiled executor's loads (index and constant tables and
+ * the x gathers): the read-only path (ld.global.nc, the default), cached in
+ * L1 (ld.global.ca) or in L2 only (ld.global.cg).  Values are the same; the
+ * choice changes which load queue the gathers wait in. */
+#define SYMGB_LOAD_READONLY 0
+#define SYMGB_LOAD_L1 1
+#define SYMGB_LOAD_L2 2
+int symgb_set_load_path(symgb_unit_t u, int path);
+
 /* Failure-handling tests only: the limit of every bounded grid-barrier wait
  * (default 2 s) and a number of arrivals each barrier waits for beyond the
  * grid (default 0; > 0 makes every barrier wait out its limit, so the run

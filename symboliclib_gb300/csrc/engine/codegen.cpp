@@ -85,7 +85,7 @@ std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, 
         if (row >= d.num_index_rows) throw std::runtime_error("codegen: index row out of range");
         if (rowVar[row] >= 0) continue;
         rowVar[row] = rows++;
-        os << "    const unsigned q" << rowVar[row] << " = __ldg(p + " << u64(d.index_offset + row * n) << " + i);\n";
+        os << "    const unsigned q" << rowVar[row] << " = SYMGB_LD(p + " << u64(d.index_offset + row * n) << " + i);\n";
     }
     for (std::uint64_t w : loads) {
         const int op = (int)(w & 0xff), dst = (int)((w >> 8) & 0xff);
@@ -97,7 +97,7 @@ std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, 
                << imm << "u)" << xs << ");\n";
         } else if (op == OP_LDC) {
             const std::string v = fresh(dst);
-            os << "    const double " << v << " = __ldg(c + " << u64(d.constants_offset + (std::uint64_t)imm * n)
+            os << "    const double " << v << " = SYMGB_LD(c + " << u64(d.constants_offset + (std::uint64_t)imm * n)
                << " + i);\n";
         } else {
             throw std::runtime_error("codegen: unknown load word");
@@ -247,8 +247,14 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
        << "\n";
     os << (cfg.kind == JIT_PERSISTENT ? "#define SYMGB_XR\n" : "#define SYMGB_XR __restrict__\n");
     os << kJitPrelude << "\n";
+    // Loads of the tables and of x: the read-only data path (ld.global.nc),
+    // cached in L1 (ld.global.ca) or in L2 only (ld.global.cg); values written
+    // earlier in the same launch (L2 = 1) always come from L2.
+    static const char* const kLoad[] = {"__ldg", "__ldca", "__ldcg"};
+    if (cfg.loadPath < 0 || cfg.loadPath > 2) throw std::runtime_error("codegen: load path must be 0, 1 or 2");
+    os << "#define SYMGB_LD(a) " << kLoad[cfg.loadPath] << "(a)\n";
     os << "template <int L2>\n__device__ __forceinline__ double symgbLoadX(const double* a) {\n"
-          "    return L2 ? __ldcg(a) : __ldg(a);\n}\n\n";
+          "    return L2 ? __ldcg(a) : SYMGB_LD(a);\n}\n\n";
     std::vector<std::size_t> opCount(descs.size());
     for (std::size_t k = 0; k < descs.size(); ++k) opCount[k] = emitBody(os, (int)k, descs[k], cfg.math, S);
     const char* params = "(const double* SYMGB_XR x, double* SYMGB_XR xw, const unsigned* __restrict__ p, "

@@ -29,6 +29,7 @@ struct JitConfig {
     std::vector<int> kernelItems;  // work items per thread, per ComputeKernel (JIT_PLAIN)
     std::vector<int> levelItems;   // per level (JIT_LEVELS); [0] for JIT_PERSISTENT
     int minBlocks = 0;  // > 0: __launch_bounds__ minimum CTAs per SM (caps registers)
+    int loadPath = 0;   // SYMGB_LOAD_*: data path of the table and x loads
 };
 
 // One launch of a module: entry name, ComputeKernel (plain) or level (levels)

@@ -254,6 +254,7 @@ JitConfig jitConfig(const symgb_unit* u, int kind) {
     c.math = u->sched.math;
     c.numSets = (unsigned)u->numSets;
     c.minBlocks = std::max(0, u->sched.blocks_per_sm);
+    c.loadPath = u->loadPath;
     for (std::size_t k = 0; k < u->kernels.size(); ++k) {
         c.kernelTpb.push_back(u->shapeOf(k).tpb);
         c.kernelItems.push_back(u->shapeOf(k).items);
@@ -287,7 +288,7 @@ std::string jitKeyOf(const JitConfig& c) {
     for (int t : c.kernelItems) k += std::to_string(t) + ",";
     k += "/";
     for (int t : c.levelItems) k += std::to_string(t) + ",";
-    k += "/" + std::to_string(c.minBlocks);
+    k += "/" + std::to_string(c.minBlocks) + "/" + std::to_string(c.loadPath);
     return k;
 }
 
@@ -845,6 +846,15 @@ int symgb_get_result_sets_async(symgb_unit_t u, double* d, int k) {
         }
     }
     SYMGB_CUDA(cudaEventRecord(u->copyDone[k], u->copyStream));
+    return SYMGB_OK;
+}
+
+int symgb_set_load_path(symgb_unit_t u, int path) {
+    if (!u || path < SYMGB_LOAD_READONLY || path > SYMGB_LOAD_L2) return fail(SYMGB_ERR_ARGUMENT, "bad load path");
+    if (path != u->loadPath) {
+        u->loadPath = path;
+        u->dropGraph();
+    }
     return SYMGB_OK;
 }
 

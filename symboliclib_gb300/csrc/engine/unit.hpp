@@ -85,6 +85,7 @@ struct symgb_unit {
     // copyStream and extraCopy[i], each chunk on its own stream so several
     // copy engines move it; extraDone[i] joins chunk i + 1 back into copyStream.
     int copyStreams = 1;
+    int loadPath = SYMGB_LOAD_READONLY;  // compiled executor's load data path (symgb_set_load_path)
     std::vector<cudaStream_t> extraCopy;
     std::vector<cudaEvent_t> extraDone;
     DevBuf<double> asyncOut;

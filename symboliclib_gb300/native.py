@@ -13,6 +13,7 @@ LIB_DIR = Path(__file__).resolve().parent / "lib"
 SCHEDULE_PLAIN, SCHEDULE_LEVELS, SCHEDULE_PERSISTENT = 0, 1, 2
 MATH_EXACT, MATH_FAST = 0, 1
 EXEC_COMPILED, EXEC_INTERPRETER = 0, 1
+LOAD_READONLY, LOAD_L1, LOAD_L2 = 0, 1, 2
 
 
 class Node(C.Structure):
@@ -114,6 +115,7 @@ SYMGB_FUNCTIONS = {
     "symgb_set_barrier_limits": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int]),
     "symgb_set_copy_streams": (C.c_int, [C.c_void_p, C.c_int]),
     "symgb_compiled_registers": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
+    "symgb_set_load_path": (C.c_int, [C.c_void_p, C.c_int]),
     "symgb_kernel_program": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]),
 }
@@ -383,6 +385,10 @@ class Unit:
         if got < 0:
             check(got)
         return list(regs)[:n]
+
+    def set_load_path(self, path: int) -> None:
+        """Data path of the compiled executor's loads (LOAD_READONLY, LOAD_L1, LOAD_L2)."""
+        check(self._lib.symgb_set_load_path(self.handle, path))
 
     def set_copy_streams(self, n: int) -> None:
         """Streams the async result copy is split over (symgb_set_copy_streams)."""

@@ -44,6 +44,7 @@ static inline double symgbFastDiv(double a, double b) { return a / b; }
 static inline double symgbFastRec(double x) { return 1.0 / x; }
 static inline double symgbFastSqrt(double x) { return std::sqrt(x); }
 template <class T> static inline T __ldg(const T* p) { return *p; }
+#define SYMGB_LD(a) (*(a))
 template <int L2> static inline double symgbLoadX(const double* a) { return *a; }
 """
 
@@ -232,3 +233,16 @@ def test_light_templates_get_an_unguarded_items_loop():
         assert "if (w0 + 192ull < " in body
     assert u.compile_check(native.SCHEDULE_PLAIN) >= 0.0
     assert u.compile_check(native.SCHEDULE_PERSISTENT) >= 0.0
+
+
+@pytest.mark.parametrize("path,intrinsic", [(0, "__ldg"), (1, "__ldca"), (2, "__ldcg")])
+def test_load_path_selects_the_load_intrinsic(path, intrinsic):
+    """symgb_set_load_path picks the data path of every table and gather load
+    of the generated module; each variant compiles for sm_103a."""
+    w = native.Workload("cotan", 8, 22)
+    u = native.Unit.from_workload(w, init=False)
+    u.set_load_path(path)
+    src = u.compiled_source(native.SCHEDULE_LEVELS)
+    assert f"#define SYMGB_LD(a) {intrinsic}(a)" in src
+    assert u.compile_check(native.SCHEDULE_LEVELS) >= 0.0
+    assert native.symgb().symgb_set_load_path(u.handle, 3) == -1

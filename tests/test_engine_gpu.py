@@ -330,3 +330,23 @@ def test_compiled_and_interpreted_per_kernel_shapes():
         assert us.shape == (u.num_kernels,) and np.all(us >= 0)
         u.run()
         assert bits_equal(u.get_result(0), gold)
+
+
+@pytest.mark.parametrize("path", [native.LOAD_READONLY, native.LOAD_L1, native.LOAD_L2])
+@pytest.mark.parametrize("kind", SCHEDULES)
+def test_compiled_load_paths(path, kind):
+    """Every load data path of the compiled executor gives the reference's
+    results bit for bit (1 and 33 value sets)."""
+    for name, size, seed in [("cotan", 8, 22), ("cloth", 5, 32), ("neohookean", 1, 41)]:
+        _, inp, gold = load_golden(name, size)
+        w = native.Workload(name, size, seed)
+        u = native.Unit.from_workload(w)
+        u.set_schedule(kind=kind, math=native.MATH_EXACT, items_per_thread=2)
+        u.set_load_path(path)
+        for sets in (1, 33):
+            u.set_num_sets(sets)
+            for i, a in enumerate(split_inputs(w, inp)):
+                u.set_arg(i, np.tile(a, sets))
+            u.run()
+            out = u.get_result(0).reshape(sets, -1)
+            assert bits_equal(out[0], gold) and bits_equal(out[-1], gold), (name, sets)
