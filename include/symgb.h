@@ -164,6 +164,19 @@ int symgb_compiled_registers(symgb_unit_t u, int kind, int* registers, int cap);
 #define SYMGB_LOAD_L2 2
 int symgb_set_load_path(symgb_unit_t u, int path);
 
+/* Which work items a thread of the compiled executor takes.
+ *   STRIDED (default): items_per_thread work items tpb apart (consecutive
+ *     threads on consecutive work items).
+ *   GROUPED: items_per_thread consecutive instances of one value set; the
+ *     thread reads their entries of each index and constant row with one
+ *     vector load (128-bit for 4 instances of an index row) from copies of
+ *     the tables whose rows are padded to a multiple of 4 entries, made on the
+ *     device at first use (about the size of the tables).
+ * Values are the same either way. */
+#define SYMGB_ITEMS_STRIDED 0
+#define SYMGB_ITEMS_GROUPED 1
+int symgb_set_item_layout(symgb_unit_t u, int layout);
+
 /* Failure-handling tests only: the limit of every bounded grid-barrier wait
  * (default 2 s) and a number of arrivals each barrier waits for beyond the
  * grid (default 0; > 0 makes every barrier wait out its limit, so the run

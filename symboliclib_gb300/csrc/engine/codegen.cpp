@@ -48,19 +48,35 @@ const char* libName(int op) {
     }
 }
 
-// Emits the device function evaluating kernel k for one work item
-// (instance i, value set s).  L2 = 1 reads x through L2 only (values written
-// earlier in the same launch, persistent schedule).  Returns the number of
-// operations of the template.
-std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, int math, unsigned S) {
+// Emits the device function evaluating kernel k.
+//   Strided items (grouped == nullptr): symgbBody<k><L2>(..., i, s) evaluates
+//     one work item (instance i, value set s) and loads its own index and
+//     constant entries.
+//   Grouped items: symgbGroup<k><L2, IT, FULL>(..., g, s) evaluates the IT
+//     consecutive instances g*IT .. g*IT+IT-1 of value set s; each index and
+//     constant row is read with one vector load from the padded copies of the
+//     tables (`grouped` gives their row bases), the instances' gathers,
+//     arithmetic and stores follow, unrolled.  FULL = false guards the
+//     instances past the kernel's end (the last group).
+// L2 = 1 reads x through L2 only (values written earlier in the same launch,
+// persistent schedule).  Returns the number of operations of the template.
+std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, int math, unsigned S,
+                     const GroupedTables* grouped) {
     std::vector<std::uint64_t> loads;
     const std::vector<LinOp> ops = linearCode(d, math, &loads);
     const std::uint64_t n = d.num_instances;
+    const bool g = grouped != nullptr;
+    const char* in = g ? "        " : "    ";
     os << "// kernel " << k << ": " << n << " instances, level " << d.level << ", " << loads.size() << " loads, "
        << ops.size() << " operations\n";
-    os << "template <int L2>\n__device__ __forceinline__ void symgbBody" << k
-       << "(const double* SYMGB_XR x, double* SYMGB_XR xw, const unsigned* __restrict__ p, "
-          "const double* __restrict__ c, unsigned long long i, unsigned s) {\n";
+    if (g)
+        os << "template <int L2, int IT, bool FULL>\n__device__ __forceinline__ void symgbGroup" << k
+           << "(const double* SYMGB_XR x, double* SYMGB_XR xw, const unsigned* __restrict__ p, "
+              "const double* __restrict__ c, unsigned long long g, unsigned s) {\n";
+    else
+        os << "template <int L2>\n__device__ __forceinline__ void symgbBody" << k
+           << "(const double* SYMGB_XR x, double* SYMGB_XR xw, const unsigned* __restrict__ p, "
+              "const double* __restrict__ c, unsigned long long i, unsigned s) {\n";
     std::vector<std::string> cur(256);
     int next = 0;
     auto fresh = [&](int reg) -> std::string {
@@ -76,7 +92,8 @@ std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, 
     };
     const std::string xs = S == 1 ? std::string() : " * " + std::to_string(S) + "ull + s";
     // Index rows read by the gathers, each loaded once (correlated index
-    // variables share a row and differ by their offsets).
+    // variables share a row and differ by their offsets); constant rows
+    // likewise in the grouped layout.
     std::vector<int> rowVar(d.num_index_rows, -1);
     int rows = 0;
     for (std::uint64_t w : loads) {
@@ -85,20 +102,46 @@ std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, 
         if (row >= d.num_index_rows) throw std::runtime_error("codegen: index row out of range");
         if (rowVar[row] >= 0) continue;
         rowVar[row] = rows++;
-        os << "    const unsigned q" << rowVar[row] << " = SYMGB_LD(p + " << u64(d.index_offset + row * n) << " + i);\n";
+        if (g)
+            os << "    unsigned q" << rowVar[row] << "[IT];\n    symgbLoadIdx<IT>(p + "
+               << u64(grouped->indexBase[k] + row * grouped->stride[k]) << " + g * IT, q" << rowVar[row] << ");\n";
+        else
+            os << "    const unsigned q" << rowVar[row] << " = SYMGB_LD(p + " << u64(d.index_offset + row * n)
+               << " + i);\n";
     }
+    std::vector<int> constVar;
+    if (g) {
+        constVar.assign(d.num_constant_rows, -1);
+        int consts = 0;
+        for (std::uint64_t w : loads) {
+            if ((int)(w & 0xff) != OP_LDC) continue;
+            const std::uint32_t row = (std::uint32_t)(w >> 32);
+            if (row >= d.num_constant_rows) throw std::runtime_error("codegen: constant row out of range");
+            if (constVar[row] >= 0) continue;
+            constVar[row] = consts++;
+            os << "    double k" << constVar[row] << "[IT];\n    symgbLoadConst<IT>(c + "
+               << u64(grouped->constBase[k] + row * grouped->stride[k]) << " + g * IT, k" << constVar[row] << ");\n";
+        }
+        os << "    #pragma unroll\n    for (int j = 0; j < IT; ++j) {\n"
+           << "        const unsigned long long i = g * IT + j;\n"
+           << "        if (!FULL && i >= " << u64(n) << ") break;\n";
+    }
+    const std::string qj = g ? "[j]" : "";
     for (std::uint64_t w : loads) {
         const int op = (int)(w & 0xff), dst = (int)((w >> 8) & 0xff);
         const std::uint32_t imm = (std::uint32_t)(w >> 32);
         if (op == OP_LDX) {
             const std::uint64_t row = (w >> 16) & 0xffff;
             const std::string v = fresh(dst);
-            os << "    const double " << v << " = symgbLoadX<L2>(x + (unsigned long long)(q" << rowVar[row] << " + "
-               << imm << "u)" << xs << ");\n";
+            os << in << "const double " << v << " = symgbLoadX<L2>(x + (unsigned long long)(q" << rowVar[row] << qj
+               << " + " << imm << "u)" << xs << ");\n";
         } else if (op == OP_LDC) {
             const std::string v = fresh(dst);
-            os << "    const double " << v << " = SYMGB_LD(c + " << u64(d.constants_offset + (std::uint64_t)imm * n)
-               << " + i);\n";
+            if (g)
+                os << in << "const double " << v << " = k" << constVar[imm] << "[j];\n";
+            else
+                os << in << "const double " << v << " = SYMGB_LD(c + "
+                   << u64(d.constants_offset + (std::uint64_t)imm * n) << " + i);\n";
         } else {
             throw std::runtime_error("codegen: unknown load word");
         }
@@ -107,7 +150,7 @@ std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, 
         std::string rhs;
         switch (L.op) {
             case OP_ST:
-                os << "    xw[(" << u64(d.output_offset + (std::uint64_t)L.row * n) << " + i)" << xs
+                os << in << "xw[(" << u64(d.output_offset + (std::uint64_t)L.row * n) << " + i)" << xs
                    << "] = " << use(L.src[0]) << ";\n";
                 continue;
             case OP_MOV: {
@@ -145,8 +188,9 @@ std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, 
             }
         }
         const std::string v = fresh(L.d);
-        os << "    const double " << v << " = " << rhs << ";\n";
+        os << in << "const double " << v << " = " << rhs << ";\n";
     }
+    if (g) os << "    }\n";
     os << "}\n\n";
     return ops.size();
 }
@@ -191,28 +235,64 @@ std::uint64_t blocksFor(std::uint64_t total, int tpb, int items) {
     return (total + per - 1) / per;
 }
 
+// Blocks of kernel k: strided, n*S work items at tpb*items per block;
+// grouped, ceil(n / items) groups per value set, one thread each.
+std::uint64_t kernelBlocks(const symgb_kernel_desc& d, unsigned S, int tpb, int items, bool grouped) {
+    if (!grouped) return blocksFor(d.num_instances * S, tpb, items);
+    const std::uint64_t groups = (d.num_instances + items - 1) / items;
+    return (groups * S + tpb - 1) / tpb;
+}
+
+// Grouped work of kernel k for block `b0` (relative to the kernel's first
+// block): thread t takes group t / S of value set t % S (consecutive threads
+// on consecutive sets, then groups).  Full groups run without per-instance
+// guards when the template is light (`split`), as in emitItems.
+void emitGroups(std::ostringstream& os, int k, const symgb_kernel_desc& d, unsigned S, int tpb, int items, int l2,
+                const std::string& b0, const char* indent, bool split) {
+    const std::uint64_t n = d.num_instances;
+    const std::uint64_t groups = (n + items - 1) / items, full = n / items;
+    os << indent << "const unsigned long long t = (" << b0 << ") * " << tpb << "ull + threadIdx.x;\n"
+       << indent << "const unsigned long long g = t / " << S << "ull;\n"
+       << indent << "const unsigned s = (unsigned)(t % " << S << "ull);\n";
+    if (split && full)
+        os << indent << "if (g < " << u64(full) << ") symgbGroup" << k << "<" << l2 << ", " << items
+           << ", true>(x, xw, p, c, g, s);\n"
+           << indent << "else if (g < " << u64(groups) << ") symgbGroup" << k << "<" << l2 << ", " << items
+           << ", false>(x, xw, p, c, g, s);\n";
+    else
+        os << indent << "if (g < " << u64(groups) << ") symgbGroup" << k << "<" << l2 << ", " << items
+           << ", false>(x, xw, p, c, g, s);\n";
+}
+
+// The work of kernel k in either item layout.
+void emitWork(std::ostringstream& os, int k, const symgb_kernel_desc& d, std::size_t ops, unsigned S, int tpb,
+              int items, int l2, const std::string& b0, const char* indent, bool grouped) {
+    const bool split = ops * (std::size_t)items <= kSplitOps;
+    if (grouped) emitGroups(os, k, d, S, tpb, items, l2, b0, indent, split);
+    else emitItems(os, k, d.num_instances * S, S, tpb, items, l2, b0, indent, split);
+}
+
 // Dispatch of block `b` over the kernels of one launch (kernel-major block
 // ranges, each kernel's work items in consecutive blocks).
 void emitDispatch(std::ostringstream& os, const std::vector<int>& ks, const std::vector<symgb_kernel_desc>& descs,
-                  const std::vector<std::size_t>& opCount, unsigned S, int tpb, int items, int l2, const char* indent) {
+                  const std::vector<std::size_t>& opCount, unsigned S, int tpb, int items, int l2, const char* indent,
+                  bool grouped) {
     std::uint64_t first = 0;
     const std::string inner = std::string(indent) + "    ";
     for (std::size_t q = 0; q < ks.size(); ++q) {
         const int k = ks[q];
-        const std::uint64_t total = descs[k].num_instances * S;
-        const std::uint64_t blocks = blocksFor(total, tpb, items);
+        const std::uint64_t blocks = kernelBlocks(descs[k], S, tpb, items, grouped);
         os << indent << (q ? "else " : "") << "if (b < " << u64(first + blocks) << ") {\n";
-        emitItems(os, k, total, S, tpb, items, l2, "b - " + u64(first), inner.c_str(),
-                  opCount[k] * (std::size_t)items <= kSplitOps);
+        emitWork(os, k, descs[k], opCount[k], S, tpb, items, l2, "b - " + u64(first), inner.c_str(), grouped);
         os << indent << "}\n";
         first += blocks;
     }
 }
 
 std::uint64_t blocksOf(const std::vector<int>& ks, const std::vector<symgb_kernel_desc>& descs, unsigned S, int tpb,
-                       int items) {
+                       int items, bool grouped) {
     std::uint64_t b = 0;
-    for (int k : ks) b += blocksFor(descs[k].num_instances * S, tpb, items);
+    for (int k : ks) b += kernelBlocks(descs[k], S, tpb, items, grouped);
     return b;
 }
 
@@ -238,10 +318,29 @@ std::string launchBounds(int tpb, int minBlocks) {
 
 }  // namespace
 
+GroupedTables groupedTables(const std::vector<symgb_kernel_desc>& descs) {
+    GroupedTables t;
+    for (const auto& d : descs) {
+        const std::uint64_t stride = (d.num_instances + 3) / 4 * 4;
+        t.stride.push_back(stride);
+        t.indexBase.push_back(t.indexSize);
+        t.constBase.push_back(t.constSize);
+        t.indexSize += stride * d.num_index_rows;
+        t.constSize += stride * d.num_constant_rows;
+    }
+    return t;
+}
+
 JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLevels, const JitConfig& cfg) {
     JitSource out;
     std::ostringstream os;
     const unsigned S = cfg.numSets;
+    if (cfg.itemLayout != SYMGB_ITEMS_STRIDED && cfg.itemLayout != SYMGB_ITEMS_GROUPED)
+        throw std::runtime_error("codegen: unknown item layout");
+    const bool grouped = cfg.itemLayout == SYMGB_ITEMS_GROUPED;
+    out.grouped = grouped;
+    GroupedTables gt;
+    if (grouped) gt = groupedTables(descs);
     os << "// symgb compiled module: " << descs.size() << " kernels, " << numLevels << " levels, " << S
        << " value sets, math " << (cfg.math == SYMGB_MATH_FAST ? "fast" : "exact") << ", schedule " << cfg.kind
        << "\n";
@@ -255,8 +354,31 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
     os << "#define SYMGB_LD(a) " << kLoad[cfg.loadPath] << "(a)\n";
     os << "template <int L2>\n__device__ __forceinline__ double symgbLoadX(const double* a) {\n"
           "    return L2 ? __ldcg(a) : SYMGB_LD(a);\n}\n\n";
+    if (grouped)
+        os << "// Entries of IT consecutive instances of one padded table row (aligned).\n"
+              "template <int IT>\n__device__ __forceinline__ void symgbLoadIdx(const unsigned* a, unsigned (&q)[IT]) {\n"
+              "    if constexpr (IT == 4) {\n"
+              "        const uint4 v = SYMGB_LD(reinterpret_cast<const uint4*>(a));\n"
+              "        q[0] = v.x; q[1] = v.y; q[2] = v.z; q[3] = v.w;\n"
+              "    } else if constexpr (IT == 2) {\n"
+              "        const uint2 v = SYMGB_LD(reinterpret_cast<const uint2*>(a));\n"
+              "        q[0] = v.x; q[1] = v.y;\n"
+              "    } else {\n"
+              "        q[0] = SYMGB_LD(a);\n"
+              "    }\n}\n"
+              "template <int IT>\n__device__ __forceinline__ void symgbLoadConst(const double* a, double (&v)[IT]) {\n"
+              "    if constexpr (IT >= 2) {\n"
+              "        #pragma unroll\n"
+              "        for (int h = 0; h < IT; h += 2) {\n"
+              "            const double2 u = SYMGB_LD(reinterpret_cast<const double2*>(a + h));\n"
+              "            v[h] = u.x; v[h + 1] = u.y;\n"
+              "        }\n"
+              "    } else {\n"
+              "        v[0] = SYMGB_LD(a);\n"
+              "    }\n}\n\n";
     std::vector<std::size_t> opCount(descs.size());
-    for (std::size_t k = 0; k < descs.size(); ++k) opCount[k] = emitBody(os, (int)k, descs[k], cfg.math, S);
+    for (std::size_t k = 0; k < descs.size(); ++k)
+        opCount[k] = emitBody(os, (int)k, descs[k], cfg.math, S, grouped ? &gt : nullptr);
     const char* params = "(const double* SYMGB_XR x, double* SYMGB_XR xw, const unsigned* __restrict__ p, "
                          "const double* __restrict__ c";
     // Kernels of each level, heaviest first (their blocks are dispatched first).
@@ -275,10 +397,11 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
             const std::string name = "symgb_k" + std::to_string(k);
             os << "extern \"C\" __global__ void " << launchBounds(tpb, cfg.minBlocks) << " " << name << params << ") {\n"
                << "    symgbDependencyWait();\n    symgbLaunchDependents();\n";
-            emitItems(os, (int)k, total, S, tpb, items, 0, "(unsigned long long)blockIdx.x", "    ",
-                      opCount[k] * (std::size_t)items <= kSplitOps);
+            emitWork(os, (int)k, descs[k], opCount[k], S, tpb, items, 0, "(unsigned long long)blockIdx.x", "    ",
+                     grouped);
             os << "}\n\n";
-            out.launches.push_back({name, (int)k, -1, blocksFor(total, tpb, items), tpb, items, false});
+            out.launches.push_back({name, (int)k, -1, kernelBlocks(descs[k], S, tpb, items, grouped), tpb, items,
+                                    false});
         }
     } else if (cfg.kind == JIT_LEVELS) {
         for (int L = 0; L < numLevels; ++L) {
@@ -293,9 +416,9 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
             os << "extern \"C\" __global__ void " << launchBounds(tpb, cfg.minBlocks) << " " << name << params << ") {\n"
                << "    symgbDependencyWait();\n    symgbLaunchDependents();\n"
                << "    const unsigned long long b = blockIdx.x;\n";
-            emitDispatch(os, ks, descs, opCount, S, tpb, items, 0, "    ");
+            emitDispatch(os, ks, descs, opCount, S, tpb, items, 0, "    ", grouped);
             os << "}\n\n";
-            out.launches.push_back({name, -1, L, blocksOf(ks, descs, S, tpb, items), tpb, items, false});
+            out.launches.push_back({name, -1, L, blocksOf(ks, descs, S, tpb, items, grouped), tpb, items, false});
         }
     } else if (cfg.kind == JIT_PERSISTENT) {
         const int tpb = cfg.levelTpb.at(0);
@@ -311,10 +434,10 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
             if (ks.empty()) continue;
             if (!firstLevel)
                 os << "    if (!symgbGridBarrier(bar, hostError, timeoutNs, gridDim.x + extra)) return;\n";
-            const std::uint64_t nb = blocksOf(ks, descs, S, tpb, items);
+            const std::uint64_t nb = blocksOf(ks, descs, S, tpb, items, grouped);
             most = std::max(most, nb);
             os << "    for (unsigned long long b = blockIdx.x; b < " << u64(nb) << "; b += gridDim.x) {\n";
-            emitDispatch(os, ks, descs, opCount, S, tpb, items, firstLevel ? 0 : 1, "        ");
+            emitDispatch(os, ks, descs, opCount, S, tpb, items, firstLevel ? 0 : 1, "        ", grouped);
             os << "    }\n";
             firstLevel = false;
         }

@@ -30,7 +30,20 @@ struct JitConfig {
     std::vector<int> levelItems;   // per level (JIT_LEVELS); [0] for JIT_PERSISTENT
     int minBlocks = 0;  // > 0: __launch_bounds__ minimum CTAs per SM (caps registers)
     int loadPath = 0;   // SYMGB_LOAD_*: data path of the table and x loads
+    int itemLayout = 0;  // SYMGB_ITEMS_*: which work items a thread takes
 };
+
+// Grouped item layout (SYMGB_ITEMS_GROUPED): copies of the index and constant
+// tables whose rows are padded to a multiple of 4 entries (the row's last
+// entry repeated), so that a thread reads the entries of 1, 2 or 4
+// consecutive instances of a row with one aligned vector load.  Kernel k's
+// row r starts at indexBase[k] + r * stride[k] (constBase[k] + r * stride[k]
+// for constants); stride[k] = n_k rounded up to a multiple of 4.
+struct GroupedTables {
+    std::vector<std::uint64_t> indexBase, constBase, stride;
+    std::uint64_t indexSize = 0, constSize = 0;  // entries of the padded copies
+};
+GroupedTables groupedTables(const std::vector<symgb_kernel_desc>& descs);
 
 // One launch of a module: entry name, ComputeKernel (plain) or level (levels)
 // it covers, blocks needed to cover its work items, block size.
@@ -47,6 +60,7 @@ struct JitLaunch {
 struct JitSource {
     std::string source;
     std::vector<JitLaunch> launches;  // in execution order
+    bool grouped = false;             // reads the padded tables (GroupedTables)
 };
 
 // Generates the module for a unit's kernels (host only; throws
@@ -60,6 +74,7 @@ struct JitModule {
     std::vector<const void*> kernels;
     std::vector<int> registers;  // per launch: registers per thread of the compiled kernel
     double compileSeconds = 0;
+    bool grouped = false;        // launch with the padded tables (GroupedTables)
 };
 
 // Compiles `source` with NVRTC without loading it (no device needed).

@@ -112,6 +112,18 @@ __global__ void __launch_bounds__(256) scatterSetsKernel(const double* __restric
     }
 }
 
+// Padded copy of one kernel's table rows for the compiled executor's grouped
+// item layout: dst[r * stride + i] = src[r * n + min(i, n - 1)] (the last
+// instance's entry fills the padding, so padded loads stay valid).
+template <class T>
+__global__ void padRowsKernel(const T* __restrict__ src, T* __restrict__ dst, std::uint64_t n, std::uint64_t stride,
+                              std::uint64_t rows) {
+    const std::uint64_t w = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= rows * stride) return;
+    const std::uint64_t r = w / stride, i = w - r * stride;
+    dst[w] = src[r * n + (i < n ? i : n - 1)];
+}
+
 // Value-set counts from which the tiled kernels are used.
 constexpr unsigned kTiledSets = 8;
 
@@ -255,6 +267,7 @@ JitConfig jitConfig(const symgb_unit* u, int kind) {
     c.numSets = (unsigned)u->numSets;
     c.minBlocks = std::max(0, u->sched.blocks_per_sm);
     c.loadPath = u->loadPath;
+    c.itemLayout = u->itemLayout;
     for (std::size_t k = 0; k < u->kernels.size(); ++k) {
         c.kernelTpb.push_back(u->shapeOf(k).tpb);
         c.kernelItems.push_back(u->shapeOf(k).items);
@@ -288,8 +301,35 @@ std::string jitKeyOf(const JitConfig& c) {
     for (int t : c.kernelItems) k += std::to_string(t) + ",";
     k += "/";
     for (int t : c.levelItems) k += std::to_string(t) + ",";
-    k += "/" + std::to_string(c.minBlocks) + "/" + std::to_string(c.loadPath);
+    k += "/" + std::to_string(c.minBlocks) + "/" + std::to_string(c.loadPath) + "/" + std::to_string(c.itemLayout);
     return k;
+}
+
+// The padded tables of the grouped item layout, made once per init on the
+// unit's stream (which is then synchronised: a later capture must not see it).
+int buildGroupedTables(symgb_unit* u) {
+    if (u->groupedBuilt) return SYMGB_OK;
+    std::vector<symgb_kernel_desc> descs;
+    for (const auto& k : u->kernels) descs.push_back(k.desc);
+    const GroupedTables t = groupedTables(descs);
+    SYMGB_CUDA(u->p4.alloc(t.indexSize));
+    SYMGB_CUDA(u->c4.alloc(t.constSize));
+    for (std::size_t k = 0; k < descs.size(); ++k) {
+        const symgb_kernel_desc& d = descs[k];
+        if (!d.num_instances) continue;
+        const std::uint64_t iw = t.stride[k] * d.num_index_rows, cw = t.stride[k] * d.num_constant_rows;
+        if (iw)
+            padRowsKernel<std::uint32_t><<<(unsigned)((iw + 255) / 256), 256, 0, u->stream>>>(
+                u->p.ptr + d.index_offset, u->p4.ptr + t.indexBase[k], d.num_instances, t.stride[k], d.num_index_rows);
+        if (cw)
+            padRowsKernel<double><<<(unsigned)((cw + 255) / 256), 256, 0, u->stream>>>(
+                u->c.ptr + d.constants_offset, u->c4.ptr + t.constBase[k], d.num_instances, t.stride[k],
+                d.num_constant_rows);
+    }
+    SYMGB_CUDA(cudaGetLastError());
+    SYMGB_CUDA(cudaStreamSynchronize(u->stream));
+    u->groupedBuilt = true;
+    return SYMGB_OK;
 }
 
 // The compiled module of schedule `kind` in the unit's current configuration,
@@ -298,6 +338,8 @@ std::string jitKeyOf(const JitConfig& c) {
 int getModule(symgb_unit* u, int kind, std::shared_ptr<const JitModule>* out, double* seconds = nullptr) {
     if (seconds) *seconds = 0.0;
     const JitConfig cfg = jitConfig(u, kind);
+    if (cfg.itemLayout == SYMGB_ITEMS_GROUPED && u->initialized)
+        if (int e = buildGroupedTables(u)) return e;
     const std::string key = jitKeyOf(cfg);
     auto it = u->jitModules.find(key);
     if (it != u->jitModules.end()) {
@@ -334,8 +376,8 @@ int enqueueCompiled(symgb_unit* u, const std::vector<cudaEvent_t>* kernelEvents)
     if (int e = getModule(u, kernelEvents ? SYMGB_SCHEDULE_PLAIN : u->sched.kind, &m)) return e;
     const double* x = u->x.ptr;
     double* xw = u->x.ptr;
-    const std::uint32_t* p = u->p.ptr;
-    const double* c = u->c.ptr;
+    const std::uint32_t* p = m->grouped ? u->p4.ptr : u->p.ptr;
+    const double* c = m->grouped ? u->c4.ptr : u->c.ptr;
     BarrierState* bar = u->barrier.ptr;
     int* hostError = u->errorDev;
     unsigned long long timeoutNs = u->barrierTimeoutNs;
@@ -846,6 +888,16 @@ int symgb_get_result_sets_async(symgb_unit_t u, double* d, int k) {
         }
     }
     SYMGB_CUDA(cudaEventRecord(u->copyDone[k], u->copyStream));
+    return SYMGB_OK;
+}
+
+int symgb_set_item_layout(symgb_unit_t u, int layout) {
+    if (!u || (layout != SYMGB_ITEMS_STRIDED && layout != SYMGB_ITEMS_GROUPED))
+        return fail(SYMGB_ERR_ARGUMENT, "bad item layout");
+    if (layout != u->itemLayout) {
+        u->itemLayout = layout;
+        u->dropGraph();
+    }
     return SYMGB_OK;
 }
 

@@ -91,6 +91,12 @@ struct symgb_unit {
     DevBuf<double> asyncOut;
     int asyncOutSets = 0;
     DevBuf<std::uint32_t> p, ids;
+    // Padded copies of p and c for the compiled executor's grouped item
+    // layout (GroupedTables), made on the device at first use.
+    int itemLayout = SYMGB_ITEMS_STRIDED;
+    DevBuf<std::uint32_t> p4;
+    DevBuf<double> c4;
+    bool groupedBuilt = false;
     DevBuf<std::uint64_t> progs;
     DevBuf<DevKernel> devKernels;
     DevBuf<Tile> tiles;
@@ -154,6 +160,9 @@ struct symgb_unit {
         outBuf.reset();
         p.reset();
         ids.reset();
+        p4.reset();
+        c4.reset();
+        groupedBuilt = false;
         progs.reset();
         devKernels.reset();
         tiles.reset();

@@ -14,6 +14,7 @@ SCHEDULE_PLAIN, SCHEDULE_LEVELS, SCHEDULE_PERSISTENT = 0, 1, 2
 MATH_EXACT, MATH_FAST = 0, 1
 EXEC_COMPILED, EXEC_INTERPRETER = 0, 1
 LOAD_READONLY, LOAD_L1, LOAD_L2 = 0, 1, 2
+ITEMS_STRIDED, ITEMS_GROUPED = 0, 1
 
 
 class Node(C.Structure):
@@ -116,6 +117,7 @@ SYMGB_FUNCTIONS = {
     "symgb_set_copy_streams": (C.c_int, [C.c_void_p, C.c_int]),
     "symgb_compiled_registers": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "symgb_set_load_path": (C.c_int, [C.c_void_p, C.c_int]),
+    "symgb_set_item_layout": (C.c_int, [C.c_void_p, C.c_int]),
     "symgb_kernel_program": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]),
 }
@@ -385,6 +387,10 @@ class Unit:
         if got < 0:
             check(got)
         return list(regs)[:n]
+
+    def set_item_layout(self, layout: int) -> None:
+        """Which work items a compiled-executor thread takes (ITEMS_STRIDED, ITEMS_GROUPED)."""
+        check(self._lib.symgb_set_item_layout(self.handle, layout))
 
     def set_load_path(self, path: int) -> None:
         """Data path of the compiled executor's loads (LOAD_READONLY, LOAD_L1, LOAD_L2)."""

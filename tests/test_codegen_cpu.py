@@ -45,6 +45,12 @@ static inline double symgbFastRec(double x) { return 1.0 / x; }
 static inline double symgbFastSqrt(double x) { return std::sqrt(x); }
 template <class T> static inline T __ldg(const T* p) { return *p; }
 #define SYMGB_LD(a) (*(a))
+template <int IT> static inline void symgbLoadIdx(const unsigned* a, unsigned (&q)[IT]) {
+    for (int j = 0; j < IT; ++j) q[j] = a[j];
+}
+template <int IT> static inline void symgbLoadConst(const double* a, double (&v)[IT]) {
+    for (int j = 0; j < IT; ++j) v[j] = a[j];
+}
 template <int L2> static inline double symgbLoadX(const double* a) { return *a; }
 """
 
@@ -100,6 +106,75 @@ def run_generated(w, inputs, math, S=1):
     for k in range(d.num_kernels):
         lib.symgb_host_run(k, x.ctypes.data, x.ctypes.data, p.ctypes.data, c.ctypes.data,
                            int(d.kernels[k].num_instances), S)
+    ids = np.asarray(w.out_index_data[int(d.output_start[0]):int(d.output_start[0]) + int(d.output_length[0])],
+                     np.int64)
+    return np.stack([x[ids * S + s] for s in range(S)])
+
+
+def grouped_host_library(source: str, num_kernels: int, items: int) -> C.CDLL:
+    """The grouped-layout bodies (symgbGroup<k>) of a generated module, for the host."""
+    start = source.index("// kernel 0:")
+    end = source.index('extern "C"')
+    bodies = source[start:end]
+    driver = ['extern "C" void symgb_host_group(int k, const double* x, double* xw, const unsigned* p, '
+              'const double* c, unsigned long long groups, unsigned S) {',
+              "    for (unsigned long long g = 0; g < groups; ++g)", "        for (unsigned s = 0; s < S; ++s)",
+              "            switch (k) {"]
+    for k in range(num_kernels):
+        if f"symgbGroup{k}(" in bodies:
+            driver.append(f"                case {k}: symgbGroup{k}<0, {items}, false>(x, xw, p, c, g, s); break;")
+    driver += ["                default: break;", "            }", "}"]
+    text = HOST_SHIM + bodies + "\n".join(driver) + "\n"
+    BUILD.mkdir(parents=True, exist_ok=True)
+    tag = hashlib.sha1(text.encode()).hexdigest()[:16]
+    src, lib = BUILD / f"g_{tag}.cpp", BUILD / f"g_{tag}.so"
+    if not lib.exists():
+        src.write_text(text)
+        subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC",
+                        str(src), "-o", str(lib)], check=True, capture_output=True)
+    h = C.CDLL(str(lib))
+    h.symgb_host_group.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint]
+    return h
+
+
+def padded_tables(w):
+    """Index and constant tables with every kernel row padded to a multiple of 4
+    entries, the last entry repeated (the grouped layout's copies)."""
+    d = w.plan.contents
+    p, c = np.asarray(w.index_data, np.uint32), np.asarray(w.const_data, np.float64)
+    p4, c4 = [], []
+    for k in range(d.num_kernels):
+        kd = d.kernels[k]
+        n = int(kd.num_instances)
+        stride = (n + 3) // 4 * 4
+        for tab, out, off, rows in ((p, p4, kd.index_offset, kd.num_index_rows),
+                                    (c, c4, kd.constants_offset, kd.num_constant_rows)):
+            for r in range(rows):
+                row = tab[off + r * n: off + (r + 1) * n]
+                out.append(np.concatenate([row, np.repeat(row[-1:], stride - n)]) if n else row)
+    cat = lambda parts, dt: np.concatenate(parts).astype(dt) if parts else np.zeros(1, dt)
+    return cat(p4, np.uint32), cat(c4, np.float64)
+
+
+def run_generated_grouped(w, inputs, math, S=1, items=4):
+    """run_generated with the grouped item layout's bodies and padded tables."""
+    u = native.Unit.from_workload(w, init=False)
+    u.set_schedule(kind=native.SCHEDULE_PLAIN, math=math, items_per_thread=items)
+    u.set_num_sets(S)
+    u.set_item_layout(native.ITEMS_GROUPED)
+    src = u.compiled_source(native.SCHEDULE_PLAIN)
+    d = w.plan.contents
+    lib = grouped_host_library(src, d.num_kernels, items)
+    x = np.zeros(int(d.num_total_memory) * S)
+    for i, a in enumerate(inputs):
+        start = int(d.arg_start[i])
+        per_set = np.asarray(a).reshape(S, -1)
+        for s in range(S):
+            x[(start + np.arange(per_set.shape[1])) * S + s] = per_set[s]
+    p4, c4 = padded_tables(w)
+    for k in range(d.num_kernels):
+        n = int(d.kernels[k].num_instances)
+        lib.symgb_host_group(k, x.ctypes.data, x.ctypes.data, p4.ctypes.data, c4.ctypes.data, (n + items - 1) // items, S)
     ids = np.asarray(w.out_index_data[int(d.output_start[0]):int(d.output_start[0]) + int(d.output_length[0])],
                      np.int64)
     return np.stack([x[ids * S + s] for s in range(S)])
@@ -246,3 +321,39 @@ def test_load_path_selects_the_load_intrinsic(path, intrinsic):
     assert f"#define SYMGB_LD(a) {intrinsic}(a)" in src
     assert u.compile_check(native.SCHEDULE_LEVELS) >= 0.0
     assert native.symgb().symgb_set_load_path(u.handle, 3) == -1
+
+
+@pytest.mark.parametrize("name,size,seed", GOLDEN_CASES)
+@pytest.mark.parametrize("items", [1, 2, 4])
+def test_grouped_bodies_reproduce_golden_results(name, size, seed, items):
+    """The grouped item layout (a thread evaluates consecutive instances, its
+    table entries read from padded rows) gives the reference's results bit
+    for bit, including the last, partial group of every kernel."""
+    _, inp, gold = load_golden(name, size)
+    w = native.Workload(name, size, seed)
+    out = run_generated_grouped(w, split_inputs(w, inp), native.MATH_EXACT, items=items)[0]
+    assert np.array_equal(out.view(np.uint64), gold.view(np.uint64))
+
+
+def test_grouped_bodies_with_value_sets_match_oracle():
+    w = native.Workload("cloth", 9, 5)
+    ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
+    out = run_generated_grouped(w, [np.tile(a, 3) for a in w.inputs], native.MATH_EXACT, S=3, items=4)
+    for s in range(3):
+        assert np.array_equal(out[s].view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.parametrize("kind", [native.SCHEDULE_PLAIN, native.SCHEDULE_LEVELS, native.SCHEDULE_PERSISTENT])
+def test_grouped_modules_compile(kind):
+    """Grouped modules compile for sm_103a in every schedule (vector loads of
+    1, 2 and 4 entries)."""
+    w = native.Workload("neohookean", 1, 41)
+    u = native.Unit.from_workload(w, init=False)
+    u.set_item_layout(native.ITEMS_GROUPED)
+    for items in (1, 2, 4):
+        u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_FAST, items_per_thread=items)
+        u.set_num_sets(1 if items < 4 else 64)
+        src = u.compiled_source(kind)
+        assert "symgbLoadIdx<IT>" in src and f", {items}, " in src
+        assert u.compile_check(kind) >= 0.0
+    assert native.symgb().symgb_set_item_layout(u.handle, 2) == -1

@@ -350,3 +350,42 @@ def test_compiled_load_paths(path, kind):
             u.run()
             out = u.get_result(0).reshape(sets, -1)
             assert bits_equal(out[0], gold) and bits_equal(out[-1], gold), (name, sets)
+
+
+@pytest.mark.parametrize("items", [1, 2, 4])
+@pytest.mark.parametrize("kind", SCHEDULES)
+def test_compiled_grouped_items(items, kind):
+    """The grouped item layout (consecutive instances per thread, vector loads
+    from padded table copies) gives the reference's results bit for bit with 1,
+    5 and 64 value sets, and switching layouts back and forth keeps them."""
+    for name, size, seed in [("cotan", 8, 22), ("cloth", 5, 32), ("neohookean", 1, 41), ("ata", 9, 12)]:
+        _, inp, gold = load_golden(name, size)
+        w = native.Workload(name, size, seed)
+        u = native.Unit.from_workload(w)
+        for layout in (native.ITEMS_GROUPED, native.ITEMS_STRIDED, native.ITEMS_GROUPED):
+            u.set_item_layout(layout)
+            u.set_schedule(kind=kind, math=native.MATH_EXACT, threads_per_block=64, items_per_thread=items)
+            for sets in (1, 5, 64):
+                u.set_num_sets(sets)
+                for i, a in enumerate(split_inputs(w, inp)):
+                    u.set_arg(i, np.tile(a, sets))
+                u.run()
+                out = u.get_result(0).reshape(sets, -1)
+                assert bits_equal(out[0], gold) and bits_equal(out[-1], gold), (name, layout, sets)
+
+
+def test_grouped_items_at_larger_sizes_match_oracle():
+    """Grouped layout on plans beyond the fixtures (partial last groups of
+    every size), exact mode against the CPU oracle."""
+    for name, size, seed in [("cotan", 61, 5), ("cloth", 13, 7), ("random", 30001, 3)]:
+        w = native.Workload(name, size, seed)
+        ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
+        u = native.Unit.from_workload(w)
+        u.set_item_layout(native.ITEMS_GROUPED)
+        for items in (2, 4):
+            for kind in SCHEDULES:
+                u.set_schedule(kind=kind, math=native.MATH_EXACT, threads_per_block=128, items_per_thread=items)
+                for i, a in enumerate(w.inputs):
+                    u.set_arg(i, a)
+                u.run()
+                assert bits_equal(u.get_result(0), ref), (name, items, kind)
