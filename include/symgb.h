@@ -171,7 +171,8 @@ int symgb_set_load_path(symgb_unit_t u, int path);
  *     thread reads their entries of each index and constant row with one
  *     vector load (128-bit for 4 instances of an index row) from copies of
  *     the tables whose rows are padded to a multiple of 4 entries, made on the
- *     device at first use (about the size of the tables).
+ *     device at first use (about the size of the tables; symgb_prepare makes
+ *     them ahead of a graph capture).
  * Values are the same either way. */
 #define SYMGB_ITEMS_STRIDED 0
 #define SYMGB_ITEMS_GROUPED 1

@@ -89,6 +89,13 @@ def test_schedule_validation():
     assert lib.symgb_set_num_sets(h, (1 << 20) + 1) == -1
     native.check(lib.symgb_set_num_sets(h, 5))
     assert lib.symgb_num_sets(h) == 5
+    for call, good, bad_values in ((lib.symgb_set_copy_streams, (1, 4, 8), (0, 9)),
+                                   (lib.symgb_set_load_path, (0, 1, 2), (-1, 3)),
+                                   (lib.symgb_set_item_layout, (0, 1), (-1, 2))):
+        for v in good:
+            native.check(call(h, v))
+        for v in bad_values:
+            assert call(h, v) == -1
     lib.symgb_unit_destroy(h)
 
 
