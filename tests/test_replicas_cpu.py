@@ -40,7 +40,7 @@ def test_step_time_is_max_over_ranks():
 
 
 def test_reference_arm_under_torchrun_prints_once():
-    """`bench.py --impl reference` launched as the driver launches N ranks:
+    """`bench.py --impl reference` launched with torchrun over N ranks:
     rank 0 alone measures and prints one JSON line; every rank exits 0."""
     pytest.importorskip("torch.distributed.run")
     port = 30500 + os.getpid() % 1000
