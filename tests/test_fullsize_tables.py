@@ -1,0 +1,34 @@
+"""The front end at benchmark size, on the CPU: the index, output-index and
+constant tables (and the seeded inputs) the engine's front end builds for
+cotan 500x500 have the SHA-256 digests of the tables the reference's own
+ComputeUnit wrote for the same workload, in its CUDA layout and in its CPU
+ComputeUnit's VecWidth(4) layout (padded, blocked tables).  The digests are
+recorded in tests/golden/reference_tables.json by
+tests/golden/make_table_hashes.py from the reference's files.  The cloth
+200x200 digests are checked with the GPU tests (test_fullsize_gpu.py), whose
+host builds that front end in a fraction of the time."""
+import hashlib
+import json
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from symboliclib_gb300 import native
+
+TABLES = ROOT / "tests" / "golden" / "reference_tables.json"
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("name,size", [("cotan", 500)])
+@pytest.mark.parametrize("layout,width", [("cuda", 0), ("cpu", 4)])
+def test_tables_equal_reference(name, size, layout, width):
+    w = native.Workload(name, size, 2024, vector_width=width)
+    ref = json.loads(TABLES.read_text())[f"{name}_{size}_{layout}"]
+    assert digest(w.index_data) == ref["indexData"]["sha256"]
+    assert digest(w.out_index_data) == ref["outIndexData"]["sha256"]
+    assert digest(w.const_data) == ref["constData"]["sha256"]
+    assert digest(np.concatenate(w.inputs)) == ref["inputs.bin"]["sha256"]
