@@ -201,6 +201,30 @@ def test_neohookean_10_exact():
             assert bits_equal(u.get_result(0), ref), (executor, kind)
 
 
+def test_ata100_stated_size():
+    """B = A^T A + A at its stated size (A 10,000 x 10,000: the 5-point stencil
+    of a 100 x 100 grid plus 2 seeded random entries per column, 69,600
+    nonzeros; B 365,700 nonzeros): exact mode bit-identical to the oracle in
+    every schedule and executor, fast mode within the tolerance, grouped items
+    too."""
+    w = native.Workload("ata", 100, 2024)
+    ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
+    u = native.Unit.from_workload(w)
+    u.set_arg(0, w.inputs[0])
+    for executor in EXECUTORS:
+        for kind in SCHEDULES:
+            u.set_schedule(kind=kind, math=native.MATH_EXACT, executor=executor)
+            u.run()
+            assert bits_equal(u.get_result(0), ref), (executor, kind)
+            u.set_schedule(kind=kind, math=native.MATH_FAST, executor=executor)
+            u.run()
+            assert rel_err(u.get_result(0), ref, 1e-10) <= 1e-12, (executor, kind)
+    u.set_item_layout(native.ITEMS_GROUPED)
+    u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_EXACT, items_per_thread=4)
+    u.run()
+    assert bits_equal(u.get_result(0), ref)
+
+
 @pytest.mark.parametrize("name,size", [("cotan", 500), ("cloth", 200)])
 def test_reference_generated_cuda_matches_engine(name, size, cotan500, cloth200, tmp_path):
     """The reference's generated CUDA for one value set, built by its own nvcc

@@ -32,3 +32,16 @@ def test_tables_equal_reference(name, size, layout, width):
     assert digest(w.out_index_data) == ref["outIndexData"]["sha256"]
     assert digest(w.const_data) == ref["constData"]["sha256"]
     assert digest(np.concatenate(w.inputs)) == ref["inputs.bin"]["sha256"]
+
+
+def test_ata100_oracle_against_numeric_model():
+    """B = A^T A + A at its stated size: the oracle (the reference's strict
+    operation order) against the FP64 numeric model (the role of Eigen's
+    numeric A^T A + A in the reference's tutorial) within 1e-11 relative, with
+    a floor of 1e-10 of the largest entry."""
+    import oracle.cpu as ocpu
+    w = native.Workload("ata", 100, 2024)
+    assert len(w.numeric) == 365700 and sum(len(a) for a in w.inputs) == 69600
+    ref = ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs)[0]
+    floor = 1e-10 * np.max(np.abs(w.numeric))
+    assert np.max(np.abs(ref - w.numeric) / np.maximum(np.abs(w.numeric), floor)) <= 1e-11
