@@ -178,6 +178,17 @@ int symgb_set_load_path(symgb_unit_t u, int path);
 #define SYMGB_ITEMS_GROUPED 1
 int symgb_set_item_layout(symgb_unit_t u, int layout);
 
+/* Direct result writes (default on): with the compiled executor and one
+ * value set, output rows whose slots no kernel reads and that each name one
+ * result position are stored by the kernels straight at their positions in
+ * the unit's result buffer (container order, the CSC order of a sparse
+ * output), instead of in x and a gather pass after the run; the results of
+ * any other rows are gathered into that buffer when they are read.  The
+ * plan is made by symgb_init.  A run waits on its stream for the unit's
+ * asynchronous result copies still reading the previous results; batch
+ * replays and symgb_time_kernels do not. */
+int symgb_set_direct_outputs(symgb_unit_t u, int on);
+
 /* Failure-handling tests only: the limit of every bounded grid-barrier wait
  * (default 2 s) and a number of arrivals each barrier waits for beyond the
  * grid (default 0; > 0 makes every barrier wait out its limit, so the run

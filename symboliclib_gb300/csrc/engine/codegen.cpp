@@ -58,10 +58,12 @@ const char* libName(int op) {
 //     tables (`grouped` gives their row bases), the instances' gathers,
 //     arithmetic and stores follow, unrolled.  FULL = false guards the
 //     instances past the kernel's end (the last group).
-// L2 = 1 reads x through L2 only (values written earlier in the same launch,
-// persistent schedule).  Returns the number of operations of the template.
+// Output rows with a start in `direct` (>= 0) store their results into
+// res[dp[start + i]] (their final positions) instead of x.  L2 = 1 reads x
+// through L2 only (values written earlier in the same launch, persistent
+// schedule).  Returns the number of operations of the template.
 std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, int math, unsigned S,
-                     const GroupedTables* grouped) {
+                     const GroupedTables* grouped, const std::vector<std::int64_t>* direct) {
     std::vector<std::uint64_t> loads;
     const std::vector<LinOp> ops = linearCode(d, math, &loads);
     const std::uint64_t n = d.num_instances;
@@ -72,11 +74,13 @@ std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, 
     if (g)
         os << "template <int L2, int IT, bool FULL>\n__device__ __forceinline__ void symgbGroup" << k
            << "(const double* SYMGB_XR x, double* SYMGB_XR xw, const unsigned* __restrict__ p, "
-              "const double* __restrict__ c, unsigned long long g, unsigned s) {\n";
+              "const double* __restrict__ c, double* __restrict__ res, const unsigned* __restrict__ dp, "
+              "unsigned long long g, unsigned s) {\n";
     else
         os << "template <int L2>\n__device__ __forceinline__ void symgbBody" << k
            << "(const double* SYMGB_XR x, double* SYMGB_XR xw, const unsigned* __restrict__ p, "
-              "const double* __restrict__ c, unsigned long long i, unsigned s) {\n";
+              "const double* __restrict__ c, double* __restrict__ res, const unsigned* __restrict__ dp, "
+              "unsigned long long i, unsigned s) {\n";
     std::vector<std::string> cur(256);
     int next = 0;
     auto fresh = [&](int reg) -> std::string {
@@ -150,8 +154,12 @@ std::size_t emitBody(std::ostringstream& os, int k, const symgb_kernel_desc& d, 
         std::string rhs;
         switch (L.op) {
             case OP_ST:
-                os << in << "xw[(" << u64(d.output_offset + (std::uint64_t)L.row * n) << " + i)" << xs
-                   << "] = " << use(L.src[0]) << ";\n";
+                if (direct && L.row < direct->size() && (*direct)[L.row] >= 0)
+                    os << in << "res[SYMGB_LD(dp + " << u64((std::uint64_t)(*direct)[L.row]) << " + i)] = "
+                       << use(L.src[0]) << ";\n";
+                else
+                    os << in << "xw[(" << u64(d.output_offset + (std::uint64_t)L.row * n) << " + i)" << xs
+                       << "] = " << use(L.src[0]) << ";\n";
                 continue;
             case OP_MOV: {
                 const std::string src = use(L.src[0]);
@@ -217,15 +225,15 @@ void emitItems(std::ostringstream& os, int k, std::uint64_t total, unsigned S, i
         os << indent << "if (w0 + " << u64((std::uint64_t)(items - 1) * tpb) << " < " << u64(total) << ") {\n"
            << indent << "    #pragma unroll\n" << indent << "    for (int j = 0; j < " << items << "; ++j) {\n"
            << indent << "        const unsigned long long w = w0 + (unsigned long long)j * " << tpb << "ull;\n"
-           << indent << "        symgbBody" << k << "<" << l2 << ">(x, xw, p, c, w / " << S << "ull, (unsigned)(w % "
-           << S << "ull));\n"
+           << indent << "        symgbBody" << k << "<" << l2 << ">(x, xw, p, c, res, dp, w / " << S
+           << "ull, (unsigned)(w % " << S << "ull));\n"
            << indent << "    }\n" << indent << "} else {\n";
     }
     if (items > 1) os << indent << "#pragma unroll\n" << indent << "for (int j = 0; j < " << items << "; ++j) {\n";
     else os << indent << "{\n" << indent << "    const int j = 0;\n";
     os << indent << "    const unsigned long long w = w0 + (unsigned long long)j * " << tpb << "ull;\n"
-       << indent << "    if (w < " << u64(total) << ") symgbBody" << k << "<" << l2 << ">(x, xw, p, c, w / " << S
-       << "ull, (unsigned)(w % " << S << "ull));\n"
+       << indent << "    if (w < " << u64(total) << ") symgbBody" << k << "<" << l2 << ">(x, xw, p, c, res, dp, w / "
+       << S << "ull, (unsigned)(w % " << S << "ull));\n"
        << indent << "}\n";
     if (items > 1 && split) os << indent << "}\n";
 }
@@ -256,12 +264,12 @@ void emitGroups(std::ostringstream& os, int k, const symgb_kernel_desc& d, unsig
        << indent << "const unsigned s = (unsigned)(t % " << S << "ull);\n";
     if (split && full)
         os << indent << "if (g < " << u64(full) << ") symgbGroup" << k << "<" << l2 << ", " << items
-           << ", true>(x, xw, p, c, g, s);\n"
+           << ", true>(x, xw, p, c, res, dp, g, s);\n"
            << indent << "else if (g < " << u64(groups) << ") symgbGroup" << k << "<" << l2 << ", " << items
-           << ", false>(x, xw, p, c, g, s);\n";
+           << ", false>(x, xw, p, c, res, dp, g, s);\n";
     else
         os << indent << "if (g < " << u64(groups) << ") symgbGroup" << k << "<" << l2 << ", " << items
-           << ", false>(x, xw, p, c, g, s);\n";
+           << ", false>(x, xw, p, c, res, dp, g, s);\n";
 }
 
 // The work of kernel k in either item layout.
@@ -377,10 +385,16 @@ JitSource generateModule(const std::vector<symgb_kernel_desc>& descs, int numLev
               "        v[0] = SYMGB_LD(a);\n"
               "    }\n}\n\n";
     std::vector<std::size_t> opCount(descs.size());
-    for (std::size_t k = 0; k < descs.size(); ++k)
-        opCount[k] = emitBody(os, (int)k, descs[k], cfg.math, S, grouped ? &gt : nullptr);
+    if (!cfg.directBase.empty() && (cfg.directBase.size() != descs.size() || S != 1))
+        throw std::runtime_error("codegen: direct result rows need one value set and a row table per kernel");
+    for (std::size_t k = 0; k < descs.size(); ++k) {
+        const std::vector<std::int64_t>* direct = cfg.directBase.empty() ? nullptr : &cfg.directBase[k];
+        if (direct)
+            for (std::int64_t b : *direct) out.direct |= b >= 0;
+        opCount[k] = emitBody(os, (int)k, descs[k], cfg.math, S, grouped ? &gt : nullptr, direct);
+    }
     const char* params = "(const double* SYMGB_XR x, double* SYMGB_XR xw, const unsigned* __restrict__ p, "
-                         "const double* __restrict__ c";
+                         "const double* __restrict__ c, double* __restrict__ res, const unsigned* __restrict__ dp";
     // Kernels of each level, heaviest first (their blocks are dispatched first).
     std::vector<std::vector<int>> byLevel(numLevels);
     for (std::size_t k = 0; k < descs.size(); ++k) {

@@ -31,6 +31,10 @@ struct JitConfig {
     int minBlocks = 0;  // > 0: __launch_bounds__ minimum CTAs per SM (caps registers)
     int loadPath = 0;   // SYMGB_LOAD_*: data path of the table and x loads
     int itemLayout = 0;  // SYMGB_ITEMS_*: which work items a thread takes
+    // Direct result writes (one value set): per kernel and output row, the
+    // row's start in the result-position table `dp` - the row's results go to
+    // res[dp[start + i]] instead of x - or -1; empty when none is direct.
+    std::vector<std::vector<std::int64_t>> directBase;
 };
 
 // Grouped item layout (SYMGB_ITEMS_GROUPED): copies of the index and constant
@@ -61,6 +65,7 @@ struct JitSource {
     std::string source;
     std::vector<JitLaunch> launches;  // in execution order
     bool grouped = false;             // reads the padded tables (GroupedTables)
+    bool direct = false;              // writes some results straight into res
 };
 
 // Generates the module for a unit's kernels (host only; throws
@@ -75,6 +80,7 @@ struct JitModule {
     std::vector<int> registers;  // per launch: registers per thread of the compiled kernel
     double compileSeconds = 0;
     bool grouped = false;        // launch with the padded tables (GroupedTables)
+    bool direct = false;         // writes some results straight into res
 };
 
 // Compiles `source` with NVRTC without loading it (no device needed).

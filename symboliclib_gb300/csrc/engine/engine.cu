@@ -124,6 +124,14 @@ __global__ void padRowsKernel(const T* __restrict__ src, T* __restrict__ dst, st
     dst[w] = src[r * n + (i < n ? i : n - 1)];
 }
 
+// res[pos[t]] = x[slot[t]]: the results of the rows that are not written
+// straight into res (one value set).
+__global__ void restGatherKernel(const double* __restrict__ x, const std::uint32_t* __restrict__ pos,
+                                 const std::uint32_t* __restrict__ slot, std::uint64_t count, double* __restrict__ res) {
+    const std::uint64_t t = (std::uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < count) res[__ldg(pos + t)] = __ldg(x + __ldg(slot + t));
+}
+
 // Value-set counts from which the tiled kernels are used.
 constexpr unsigned kTiledSets = 8;
 
@@ -268,6 +276,7 @@ JitConfig jitConfig(const symgb_unit* u, int kind) {
     c.minBlocks = std::max(0, u->sched.blocks_per_sm);
     c.loadPath = u->loadPath;
     c.itemLayout = u->itemLayout;
+    if (u->directOutputs && u->numSets == 1 && u->directRows) c.directBase = u->directBase;
     for (std::size_t k = 0; k < u->kernels.size(); ++k) {
         c.kernelTpb.push_back(u->shapeOf(k).tpb);
         c.kernelItems.push_back(u->shapeOf(k).items);
@@ -301,7 +310,8 @@ std::string jitKeyOf(const JitConfig& c) {
     for (int t : c.kernelItems) k += std::to_string(t) + ",";
     k += "/";
     for (int t : c.levelItems) k += std::to_string(t) + ",";
-    k += "/" + std::to_string(c.minBlocks) + "/" + std::to_string(c.loadPath) + "/" + std::to_string(c.itemLayout);
+    k += "/" + std::to_string(c.minBlocks) + "/" + std::to_string(c.loadPath) + "/" + std::to_string(c.itemLayout) +
+         "/" + std::to_string(c.directBase.empty() ? 0 : 1);
     return k;
 }
 
@@ -378,12 +388,15 @@ int enqueueCompiled(symgb_unit* u, const std::vector<cudaEvent_t>* kernelEvents)
     double* xw = u->x.ptr;
     const std::uint32_t* p = m->grouped ? u->p4.ptr : u->p.ptr;
     const double* c = m->grouped ? u->c4.ptr : u->c.ptr;
+    double* res = m->direct ? u->res.ptr : nullptr;
+    const std::uint32_t* dp = m->direct ? u->dp.ptr : nullptr;
     BarrierState* bar = u->barrier.ptr;
     int* hostError = u->errorDev;
     unsigned long long timeoutNs = u->barrierTimeoutNs;
     unsigned extra = u->barrierExtra;
-    void* args[] = {(void*)&x, (void*)&xw, (void*)&p, (void*)&c, (void*)&bar, (void*)&hostError, (void*)&timeoutNs,
-                    (void*)&extra};
+    void* args[] = {(void*)&x,   (void*)&xw,  (void*)&p,         (void*)&c,         (void*)&res,
+                    (void*)&dp,  (void*)&bar, (void*)&hostError, (void*)&timeoutNs, (void*)&extra};
+
     int launches = 0;
     for (std::size_t j = 0; j < m->launches.size(); ++j) {
         const JitLaunch& L = m->launches[j];
@@ -418,6 +431,7 @@ int enqueueCompiled(symgb_unit* u, const std::vector<cudaEvent_t>* kernelEvents)
         ++launches;
     }
     u->launchesPerRun = launches;
+    u->lastRunDirect = m->direct;
     return SYMGB_OK;
 }
 
@@ -426,6 +440,7 @@ int enqueueCompiled(symgb_unit* u, const std::vector<cudaEvent_t>* kernelEvents)
 // each kernel's launch (per-kernel timing).
 int enqueueRun(symgb_unit* u, const std::vector<cudaEvent_t>* kernelEvents = nullptr) {
     if (u->compiledExec()) return enqueueCompiled(u, kernelEvents);
+    u->lastRunDirect = false;
     if (int e = buildTiles(u)) return e;
     const int items = u->items();
     const int tpb = u->launchTpb();
@@ -549,6 +564,11 @@ int enqueueRun(symgb_unit* u, const std::vector<cudaEvent_t>* kernelEvents = nul
 
 int runAsync(symgb_unit* u) {
     if (!u->initialized) return fail(SYMGB_ERR_STATE, "run before init");
+    // A run that writes its results straight into res waits (on the unit's
+    // stream) for the asynchronous copies still reading the previous ones.
+    if (u->compiledExec() && u->directOutputs && u->directRows && u->numSets == 1)
+        for (cudaEvent_t e : u->copyDone)
+            if (e) SYMGB_CUDA(cudaStreamWaitEvent(u->stream, e, 0));
     if (u->sched.use_graph) {
         if (!u->graphValid) {
             if (u->compiledExec()) {  // nothing may be compiled or loaded during the capture
@@ -654,7 +674,10 @@ int symgb_init(symgb_unit_t u, const uint32_t* index_data, const uint32_t* out_i
     if (!u) return fail(SYMGB_ERR_ARGUMENT, "null unit");
     if ((u->numIndices && !index_data) || (u->numOutputValues && !out_index_data) || (u->numConstants && !const_data))
         return fail(SYMGB_ERR_ARGUMENT, "null table");
-    // Every index must address x; checked once here so the kernels need no bounds checks.
+    // Every index must address x; checked once here so the kernels need no
+    // bounds checks.  The slots some kernel reads are noted for the direct
+    // result plan.
+    std::vector<std::uint8_t> slotRead(u->numTotalMemory, 0);
     for (const auto& k : u->kernels) {
         const auto& d = k.desc;
         for (std::uint32_t a = 0; a < d.num_access; ++a) {
@@ -665,12 +688,63 @@ int symgb_init(symgb_unit_t u, const uint32_t* index_data, const uint32_t* out_i
                 const long long slot = (long long)pr[i] + off;
                 if (slot < 0 || (std::uint64_t)slot >= u->numTotalMemory)
                     return fail(SYMGB_ERR_ARGUMENT, "index table entry outside x");
+                slotRead[(std::size_t)slot] = 1;
             }
         }
     }
     for (std::uint64_t j = 0; j < u->numOutputValues; ++j)
         if (out_index_data[j] >= u->numTotalMemory) return fail(SYMGB_ERR_ARGUMENT, "output id outside x");
     u->release();
+    u->jitModules.clear();  // their direct result rows belong to the previous tables
+    // Direct result plan: an output row is direct when each of its slots is
+    // read by no kernel and is the slot of exactly one result position.
+    {
+        constexpr std::uint32_t kNone = 0xffffffffu, kMany = 0xfffffffeu;
+        std::vector<std::uint32_t> posOf(u->numTotalMemory, kNone);
+        for (std::uint64_t j = 0; j < u->numOutputValues; ++j) {
+            std::uint32_t& q = posOf[out_index_data[j]];
+            q = q == kNone ? (std::uint32_t)j : kMany;
+        }
+        std::vector<std::uint8_t> covered(u->numOutputValues, 0);
+        std::vector<std::uint32_t> dpHost;
+        u->directBase.assign(u->kernels.size(), {});
+        for (std::size_t k = 0; k < u->kernels.size(); ++k) {
+            const auto& d = u->kernels[k].desc;
+            const std::uint64_t n = d.num_instances;
+            u->directBase[k].assign(d.num_output_rows, -1);
+            for (std::uint32_t r = 0; r < d.num_output_rows && n; ++r) {
+                const std::uint64_t base = d.output_offset + (std::uint64_t)r * n;
+                bool ok = true;
+                for (std::uint64_t i = 0; i < n && ok; ++i)
+                    ok = !slotRead[base + i] && posOf[base + i] < kMany;
+                if (!ok) continue;
+                u->directBase[k][r] = (std::int64_t)dpHost.size();
+                for (std::uint64_t i = 0; i < n; ++i) {
+                    dpHost.push_back(posOf[base + i]);
+                    covered[posOf[base + i]] = 1;
+                }
+            }
+        }
+        std::vector<std::uint32_t> restPos, restSlot;
+        for (std::uint64_t j = 0; j < u->numOutputValues; ++j)
+            if (!covered[j]) {
+                restPos.push_back((std::uint32_t)j);
+                restSlot.push_back(out_index_data[j]);
+            }
+        u->directRows = !dpHost.empty();
+        u->restCount = restPos.size();
+        if (u->directRows) {
+            SYMGB_CUDA(u->dp.alloc(dpHost.size()));
+            SYMGB_CUDA(cudaMemcpy(u->dp.ptr, dpHost.data(), dpHost.size() * 4, cudaMemcpyHostToDevice));
+            SYMGB_CUDA(u->res.alloc(u->numOutputValues));
+            if (u->restCount) {
+                SYMGB_CUDA(u->restPos.alloc(u->restCount));
+                SYMGB_CUDA(u->restSlot.alloc(u->restCount));
+                SYMGB_CUDA(cudaMemcpy(u->restPos.ptr, restPos.data(), u->restCount * 4, cudaMemcpyHostToDevice));
+                SYMGB_CUDA(cudaMemcpy(u->restSlot.ptr, restSlot.data(), u->restCount * 4, cudaMemcpyHostToDevice));
+            }
+        }
+    }
     SYMGB_CUDA(cudaGetDevice(&u->device));
     SYMGB_CUDA(cudaDeviceGetAttribute(&u->smCount, cudaDevAttrMultiProcessorCount, u->device));
     int optin = 0;
@@ -730,9 +804,32 @@ static int ensureOutBuf(symgb_unit* u, std::size_t n) {
     return SYMGB_OK;
 }
 
+// When the last run wrote its results straight into res (compiled executor,
+// one value set), completes res with the other rows' results on the unit's
+// stream and returns true: the results are then read from res.
+static bool resultsInRes(symgb_unit* u, int* err) {
+    *err = SYMGB_OK;
+    if (!u->lastRunDirect || u->numSets != 1) return false;
+    if (u->restCount) {
+        restGatherKernel<<<(unsigned)((u->restCount + 255) / 256), 256, 0, u->stream>>>(
+            u->x.ptr, u->restPos.ptr, u->restSlot.ptr, u->restCount, u->res.ptr);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) *err = fail(SYMGB_ERR_CUDA, std::string("rest gather: ") + cudaGetErrorString(e));
+    }
+    return true;
+}
+
 int symgb_get_result_sets_device(symgb_unit_t u, double* d, int k) {
     if (!u || !u->initialized) return fail(SYMGB_ERR_STATE, "get_result before init");
     if (k < 0 || (std::size_t)k >= u->outStart.size() || !d) return fail(SYMGB_ERR_ARGUMENT, "bad result index");
+    int err = SYMGB_OK;
+    if (resultsInRes(u, &err)) {
+        if (err) return err;
+        if (u->outLength[k])
+            SYMGB_CUDA(cudaMemcpyAsync(d, u->res.ptr + u->outStart[k], u->outLength[k] * 8, cudaMemcpyDefault,
+                                       u->stream));
+        return SYMGB_OK;
+    }
     const std::uint64_t len = u->outLength[k];
     const std::uint64_t work = len * u->numSets;
     if (work && u->numSets >= kTiledSets) {
@@ -769,6 +866,13 @@ int symgb_get_result_sets(symgb_unit_t u, double* d, int k) {
         return checkDeviceError(u);
     }
     const std::size_t n = u->outLength[k] * (std::size_t)u->numSets;
+    int err = SYMGB_OK;
+    if (resultsInRes(u, &err)) {
+        if (err) return err;
+        if (n) SYMGB_CUDA(cudaMemcpyAsync(d, u->res.ptr + u->outStart[k], n * 8, cudaMemcpyDeviceToHost, u->stream));
+        SYMGB_CUDA(cudaStreamSynchronize(u->stream));
+        return checkDeviceError(u);
+    }
     if (int e = ensureOutBuf(u, n)) return e;
     if (int e = symgb_get_result_sets_device(u, u->outBuf.ptr, k)) return e;
     SYMGB_CUDA(cudaMemcpyAsync(d, u->outBuf.ptr, n * 8, cudaMemcpyDeviceToHost, u->stream));
@@ -863,7 +967,15 @@ int symgb_get_result_sets_async(symgb_unit_t u, double* d, int k) {
     } else {
         SYMGB_CUDA(cudaEventCreateWithFlags(&u->copyDone[k], cudaEventDisableTiming));
     }
-    if (int e = symgb_get_result_sets_device(u, buf, k)) return e;
+    // Results written straight into res are copied from there (the next run
+    // waits for this copy before it rewrites res).
+    int err = SYMGB_OK;
+    if (resultsInRes(u, &err)) {
+        if (err) return err;
+        buf = u->res.ptr + u->outStart[k];
+    } else if (int e = symgb_get_result_sets_device(u, buf, k)) {
+        return e;
+    }
     SYMGB_CUDA(cudaEventRecord(u->gatherDone, u->stream));
     // Chunks of at least 8 MiB, one per copy stream in use.
     const std::size_t minChunk = (8u << 20) / 8;
@@ -888,6 +1000,15 @@ int symgb_get_result_sets_async(symgb_unit_t u, double* d, int k) {
         }
     }
     SYMGB_CUDA(cudaEventRecord(u->copyDone[k], u->copyStream));
+    return SYMGB_OK;
+}
+
+int symgb_set_direct_outputs(symgb_unit_t u, int on) {
+    if (!u || (on != 0 && on != 1)) return fail(SYMGB_ERR_ARGUMENT, "direct outputs must be 0 or 1");
+    if ((bool)on != u->directOutputs) {
+        u->directOutputs = on;
+        u->dropGraph();
+    }
     return SYMGB_OK;
 }
 

@@ -124,6 +124,7 @@ int loadModule(const JitSource& src, std::shared_ptr<const JitModule>* out, std:
     auto m = std::make_shared<JitModule>();
     m->launches = src.launches;
     m->grouped = src.grouped;
+    m->direct = src.direct;
     for (const JitLaunch& L : src.launches) {
         cudaKernel_t k;
         ce = cudaLibraryGetKernel(&k, e.library, L.name.c_str());

@@ -97,6 +97,20 @@ struct symgb_unit {
     DevBuf<std::uint32_t> p4;
     DevBuf<double> c4;
     bool groupedBuilt = false;
+    // Direct result writes of the compiled executor with one value set
+    // (symgb_set_direct_outputs), planned at init: output rows whose slots no
+    // kernel reads and that each name one result position are stored straight
+    // into `res` at those positions - directBase[k][row] is the row's start in
+    // dp (the positions, [row][instance]) or -1 - and the results of the other
+    // rows are gathered into `res` (restPos / restSlot pairs) when they are
+    // read.  lastRunDirect: the last enqueued run wrote res.
+    bool directOutputs = true;
+    bool directRows = false;  // some row is direct
+    std::vector<std::vector<std::int64_t>> directBase;
+    DevBuf<std::uint32_t> dp, restPos, restSlot;
+    std::uint64_t restCount = 0;
+    DevBuf<double> res;
+    bool lastRunDirect = false;
     DevBuf<std::uint64_t> progs;
     DevBuf<DevKernel> devKernels;
     DevBuf<Tile> tiles;
@@ -163,6 +177,14 @@ struct symgb_unit {
         p4.reset();
         c4.reset();
         groupedBuilt = false;
+        dp.reset();
+        restPos.reset();
+        restSlot.reset();
+        res.reset();
+        directRows = false;
+        directBase.clear();
+        restCount = 0;
+        lastRunDirect = false;
         progs.reset();
         devKernels.reset();
         tiles.reset();

@@ -118,6 +118,7 @@ SYMGB_FUNCTIONS = {
     "symgb_compiled_registers": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "symgb_set_load_path": (C.c_int, [C.c_void_p, C.c_int]),
     "symgb_set_item_layout": (C.c_int, [C.c_void_p, C.c_int]),
+    "symgb_set_direct_outputs": (C.c_int, [C.c_void_p, C.c_int]),
     "symgb_kernel_program": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]),
 }
@@ -387,6 +388,10 @@ class Unit:
         if got < 0:
             check(got)
         return list(regs)[:n]
+
+    def set_direct_outputs(self, on: bool) -> None:
+        """Results written straight at their positions (symgb_set_direct_outputs)."""
+        check(self._lib.symgb_set_direct_outputs(self.handle, int(on)))
 
     def set_item_layout(self, layout: int) -> None:
         """Which work items a compiled-executor thread takes (ITEMS_STRIDED, ITEMS_GROUPED)."""

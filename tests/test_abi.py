@@ -91,7 +91,8 @@ def test_schedule_validation():
     assert lib.symgb_num_sets(h) == 5
     for call, good, bad_values in ((lib.symgb_set_copy_streams, (1, 4, 8), (0, 9)),
                                    (lib.symgb_set_load_path, (0, 1, 2), (-1, 3)),
-                                   (lib.symgb_set_item_layout, (0, 1), (-1, 2))):
+                                   (lib.symgb_set_item_layout, (0, 1), (-1, 2)),
+                                   (lib.symgb_set_direct_outputs, (0, 1), (-1, 2))):
         for v in good:
             native.check(call(h, v))
         for v in bad_values:

@@ -66,7 +66,7 @@ def host_library(source: str, num_kernels: int) -> C.CDLL:
               "            switch (k) {"]
     for k in range(num_kernels):
         if f"symgbBody{k}(" in bodies:
-            driver.append(f"                case {k}: symgbBody{k}<0>(x, xw, p, c, i, s); break;")
+            driver.append(f"                case {k}: symgbBody{k}<0>(x, xw, p, c, nullptr, nullptr, i, s); break;")
     driver += ["                default: break;", "            }", "}"]
     text = HOST_SHIM + bodies + "\n".join(driver) + "\n"
     BUILD.mkdir(parents=True, exist_ok=True)
@@ -122,7 +122,8 @@ def grouped_host_library(source: str, num_kernels: int, items: int) -> C.CDLL:
               "            switch (k) {"]
     for k in range(num_kernels):
         if f"symgbGroup{k}(" in bodies:
-            driver.append(f"                case {k}: symgbGroup{k}<0, {items}, false>(x, xw, p, c, g, s); break;")
+            driver.append(f"                case {k}: symgbGroup{k}<0, {items}, false>(x, xw, p, c, nullptr, nullptr, g, s);"
+                          " break;")
     driver += ["                default: break;", "            }", "}"]
     text = HOST_SHIM + bodies + "\n".join(driver) + "\n"
     BUILD.mkdir(parents=True, exist_ok=True)

@@ -8,6 +8,8 @@ and 1e-4 for the assembled matrices (cotangent Laplacian, cloth and
 Neo-Hookean Hessians), whose small entries are sums of terms up to ~1e4 times
 larger than the result (contraction rounds those terms
 differently; an exact emulation of the FMA program gives the same error)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -390,3 +392,73 @@ def test_grouped_items_at_larger_sizes_match_oracle():
                     u.set_arg(i, a)
                 u.run()
                 assert bits_equal(u.get_result(0), ref), (name, items, kind)
+
+
+def duplicated_output_plan(w, count=10):
+    """The workload's plan with a second output container that repeats the
+    first `count` results (their slots then name two result positions, so
+    their rows cannot be written straight into the result buffer)."""
+    d = w.plan.contents
+    n0 = int(d.output_length[0])
+    desc = native.PlanDesc()
+    for name, _ in native.PlanDesc._fields_:
+        setattr(desc, name, getattr(d, name))
+    starts = (C.c_uint64 * 2)(0, n0)
+    lengths = (C.c_uint64 * 2)(n0, count)
+    desc.num_outputs, desc.output_start, desc.output_length = 2, starts, lengths
+    desc.num_output_values = n0 + count
+    ids = np.concatenate([w.out_index_data[:n0], w.out_index_data[:count]]).astype(np.uint32)
+    return desc, (starts, lengths), ids
+
+
+
+@pytest.mark.parametrize("kind", SCHEDULES)
+def test_direct_outputs_match_the_gathered_results(kind):
+    """Results written straight at their positions (the default with the
+    compiled executor and one value set) equal the gathered ones bit for bit,
+    through every read path: host, page-locked, device and asynchronous."""
+    torch = pytest.importorskip("torch")
+    lib = native.symgb()
+    for name, size, seed in [("cotan", 8, 22), ("cloth", 5, 32), ("neohookean", 1, 41), ("ata", 9, 12)]:
+        _, inp, gold = load_golden(name, size)
+        w = native.Workload(name, size, seed)
+        u = native.Unit.from_workload(w)
+        u.set_schedule(kind=kind, math=native.MATH_EXACT)
+        for i, a in enumerate(split_inputs(w, inp)):
+            u.set_arg(i, a)
+        for direct in (False, True):
+            u.set_direct_outputs(direct)
+            u.run()
+            assert bits_equal(u.get_result(0), gold), (name, direct)
+            pinned = torch.full((len(gold),), -1.0, dtype=torch.float64).pin_memory()
+            native.check(lib.symgb_get_result_sets(u.handle, C.c_void_p(pinned.data_ptr()), 0))
+            assert bits_equal(pinned.numpy(), gold), (name, direct)
+            dev = torch.full((len(gold),), -1.0, dtype=torch.float64, device="cuda")
+            native.check(lib.symgb_get_result_sets_device(u.handle, C.c_void_p(dev.data_ptr()), 0))
+            native.check(lib.symgb_synchronize(u.handle))
+            assert bits_equal(dev.cpu().numpy(), gold), (name, direct)
+            outs = [torch.full((len(gold),), -1.0, dtype=torch.float64).pin_memory() for _ in range(3)]
+            for o in outs:
+                native.check(lib.symgb_run_async(u.handle))
+                native.check(lib.symgb_get_result_sets_async(u.handle, C.c_void_p(o.data_ptr()), 0))
+            native.check(lib.symgb_synchronize(u.handle))
+            for o in outs:
+                assert bits_equal(o.numpy(), gold), (name, direct)
+
+
+def test_direct_outputs_with_shared_result_slots():
+    """A plan whose second output container repeats results of the first: the
+    rows holding the shared slots are gathered into the result buffer, the
+    others written straight; both containers come out right, also after a
+    graph replay and with an interpreter run in between."""
+    _, inp, gold = load_golden("cotan", 8)
+    w = native.Workload("cotan", 8, 22)
+    desc, keep, ids = duplicated_output_plan(w)
+    u = native.Unit(C.pointer(desc), w.index_data, ids, w.const_data)
+    for executor, graph in ((native.EXEC_COMPILED, 0), (native.EXEC_INTERPRETER, 0), (native.EXEC_COMPILED, 1)):
+        u.set_schedule(kind=native.SCHEDULE_LEVELS, math=native.MATH_EXACT, executor=executor, use_graph=graph)
+        for i, a in enumerate(split_inputs(w, inp)):
+            u.set_arg(i, a)
+        u.run()
+        assert bits_equal(u.get_result(0), gold), (executor, graph)
+        assert bits_equal(u.get_result(1), gold[:10]), (executor, graph)
