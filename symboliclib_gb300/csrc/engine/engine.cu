@@ -697,8 +697,9 @@ int symgb_init(symgb_unit_t u, const uint32_t* index_data, const uint32_t* out_i
     u->release();
     u->jitModules.clear();  // their direct result rows belong to the previous tables
     // Direct result plan: an output row is direct when each of its slots is
-    // read by no kernel and is the slot of exactly one result position.
-    {
+    // read by no kernel and is the slot of exactly one result position
+    // (positions are 32-bit in the table: larger result sets are gathered).
+    if (u->numOutputValues < 0xfffffffeull) {
         constexpr std::uint32_t kNone = 0xffffffffu, kMany = 0xfffffffeu;
         std::vector<std::uint32_t> posOf(u->numTotalMemory, kNone);
         for (std::uint64_t j = 0; j < u->numOutputValues; ++j) {
