@@ -185,8 +185,12 @@ long long liveNodeCount() {
     return n;
 }
 
+// One counter per thread: the expressions a thread builds are numbered as a
+// program that builds them alone numbers them, whatever other threads build
+// at the same time (several front ends may run side by side; the worker
+// pool's threads never draw from it).
 int& Symbolic::uniqueVariableCounter() {
-    static int counter = 0;
+    static thread_local int counter = 0;
     return counter;
 }
 

@@ -137,14 +137,18 @@ def batch(args):
     rng = np.random.default_rng(args.seed)
     sides = np.exp(rng.uniform(math.log(args.min_side), math.log(args.max_side), args.count)).round().astype(int)
     sets = rng.integers(1, args.max_sets + 1, args.count)
-    cache = {}
     t0 = time.perf_counter()
+    # one plan per distinct side (the pattern cache), built by several front
+    # ends side by side, largest first
+    from concurrent.futures import ThreadPoolExecutor
+    distinct = sorted({int(x) for x in sides}, reverse=True)
+    with ThreadPoolExecutor(max_workers=max(1, args.build_workers)) as ex:
+        built = ex.map(lambda side: native.Workload("cloth", side, args.seed + side), distinct)
+        cache = dict(zip(distinct, built))
     units, total_nnz, plain_s = [], 0, 0.0
     flush = flush_buffer()
     for k, (side, S) in enumerate(zip(sides, sets)):
-        if side not in cache:
-            cache[side] = native.Workload("cloth", int(side), args.seed + int(side))
-        w = cache[side]
+        w = cache[int(side)]
         u = native.Unit.from_workload(w)
         units.append((u, int(S), w))
         total_nnz += len(w.numeric) * int(S)
@@ -417,6 +421,7 @@ def main():
     b.add_argument("--tpb", type=int, default=64)
     b.add_argument("--seed", type=int, default=7)
     b.add_argument("--steps", type=int, default=10)
+    b.add_argument("--build-workers", type=int, default=4, help="front ends building patterns side by side")
     c = sub.add_parser("learned")
     c.add_argument("--target", default="neohookean")
     c.add_argument("--target-size", type=int, default=6)
