@@ -936,10 +936,11 @@ int symgb_set_arg_sets_async(symgb_unit_t u, const double* d, int i) {
     return symgb_set_arg_sets_device(u, u->staging.ptr, i);
 }
 
-// The result is gathered on the unit's stream into a device buffer and copied
-// to the host by the copy engine on the unit's copy stream, which the unit's
-// stream does not wait for: the next execute's input copy and evaluation
-// overlap this one's result copy.  (Gathering straight into page-locked memory
+// The result is gathered on the unit's stream into a device buffer (or, when
+// the run wrote it straight into res, taken from there) and copied to the
+// host by the copy engine on the unit's copy stream, which the unit's stream
+// does not wait for: the next execute's input copy and evaluation overlap
+// this one's result copy.  (Gathering straight into page-locked memory
 // would hold SMs for the whole transfer over the host link.)
 int symgb_get_result_sets_async(symgb_unit_t u, double* d, int k) {
     if (!u || !u->initialized) return fail(SYMGB_ERR_STATE, "get_result before init");
