@@ -13,13 +13,18 @@
 // the plan to the GPU instead of generating and building source code.
 //
 // Differences from the reference, by design: RealT must be double (the engine
-// evaluates in FP64); errors throw std::runtime_error instead of exiting the
-// process; several units can be live at once (no fixed file names).  Engine
+// evaluates in FP64); an engine error throws std::runtime_error by default
+// instead of exiting the process - OnError(ErrorPolicy::Print) prints it and
+// carries on, OnError(ErrorPolicy::Exit) prints it and exits as the
+// reference's generated library does (StringResources.h:28-34); several units
+// can be live at once (no fixed file names).  Engine
 // extensions: ValueSets(S) evaluates S value sets per execute (inputs and
 // results hold S consecutive copies of each container), ExactMath() selects
 // the bit-exact mode, and PlainSchedule / LevelSchedule / PersistentSchedule
 // choose the launch structure.
 #pragma once
+#include <cstdio>
+#include <cstdlib>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -47,6 +52,10 @@ using DecompositionThreshold = NamedType<int, struct DecompositionThresholdTag>;
 using ValueSets = NamedType<int, struct ValueSetsTag>;
 using ItemsPerThread = NamedType<int, struct ItemsPerThreadTag>;
 
+// What the ComputeUnit does when an engine call fails.
+enum class ErrorPolicy { Throw, Print, Exit };
+using OnError = NamedType<ErrorPolicy, struct OnErrorTag>;
+
 struct UseCuda {};
 struct UseHIP {};
 struct UseSinglePrecision {};
@@ -68,6 +77,7 @@ public:
     int math = SYMGB_MATH_FAST;
     int schedule = SYMGB_SCHEDULE_LEVELS;
     int itemsPerThread = 1;
+    ErrorPolicy onError = ErrorPolicy::Throw;
 
     template <class... Args>
     explicit Device(const Args&... args) {
@@ -87,6 +97,7 @@ private:
     void set(const NumThreads& v) { numThreads = (unsigned)v.x; }
     void set(const ValueSets& v) { valueSets = v.x; }
     void set(const ItemsPerThread& v) { itemsPerThread = v.x; }
+    void set(const OnError& v) { onError = v.x; }
     void set(const UseSinglePrecision&) { singlePrecision = true; }
     void set(const UseHIP&) { throw std::invalid_argument("UseHIP: the GB300 engine runs CUDA only"); }
     void set(const UseCuda&) {
@@ -202,8 +213,12 @@ public:
     const symgb_plan_desc& planDesc() const { return image_.desc; }
 
 private:
-    static void check(int rc) {
-        if (rc != SYMGB_OK) throw std::runtime_error(std::string("symgb: ") + symgb_last_error());
+    void check(int rc) const {
+        if (rc == SYMGB_OK) return;
+        const std::string msg = std::string("symgb: ") + symgb_last_error();
+        if (device_.onError == ErrorPolicy::Throw) throw std::runtime_error(msg);
+        std::fprintf(stderr, "%s\n", msg.c_str());
+        if (device_.onError == ErrorPolicy::Exit) std::exit(EXIT_FAILURE);
     }
     void requireCompiled() const {
         if (!unit_) throw std::logic_error("ComputeUnit: compile() first");

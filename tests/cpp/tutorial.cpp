@@ -49,6 +49,33 @@ int main(int argc, char** argv) {
         rejected = true;
     }
     expect(rejected, "ThreadsPerBlock(100) rejected", rejected, 1.0);
+    // An engine error (here ValueSets(0), refused by symgb_set_num_sets) throws
+    // by default; with OnError(ErrorPolicy::Print) it is printed and compile()
+    // returns; with OnError(ErrorPolicy::Exit) the process exits (--exit-policy).
+    {
+        bool threw = false;
+        try {
+            ComputeUnit<double> bad(Device(UseCuda(), ValueSets(0)), AS, BS.values);
+            bad.compile();
+        } catch (const std::runtime_error&) {
+            threw = true;
+        }
+        expect(threw, "engine error throws by default", threw, 1.0);
+        bool printed = true;
+        try {
+            ComputeUnit<double> quiet(Device(UseCuda(), ValueSets(0), OnError(ErrorPolicy::Print)), AS, BS.values);
+            quiet.compile();
+        } catch (const std::exception&) {
+            printed = false;
+        }
+        expect(printed, "OnError(Print) carries on", printed, 1.0);
+        if (argc > 1 && std::strcmp(argv[1], "--exit-policy") == 0) {
+            ComputeUnit<double> fatal(Device(UseCuda(), ValueSets(0), OnError(ErrorPolicy::Exit)), AS, BS.values);
+            fatal.compile();
+            std::printf("not reached\n");
+            return 0;
+        }
+    }
     if (gpu) {
         std::vector<double> B(BS.nnz(), 0.0);
         unit.compile().execute(A.values).getResults(B);

@@ -28,6 +28,15 @@ def test_tutorial_known_answers(tutorial_binary):
     assert r.returncode == 0, r.stdout + r.stderr
 
 
+def test_exit_error_policy_exits_like_the_reference(tutorial_binary):
+    """OnError(ErrorPolicy::Exit): an engine error prints the message and ends
+    the process with a failure status, as the reference's generated library
+    does; the default policy throws and Print carries on (checked inside)."""
+    r = subprocess.run([str(tutorial_binary), "--exit-policy"], capture_output=True, text=True)
+    assert r.returncode == 1, r.stdout + r.stderr
+    assert "symgb:" in r.stderr and "not reached" not in r.stdout
+
+
 @pytest.mark.gpu
 def test_compute_unit_round_trip(tutorial_binary):
     r = subprocess.run([str(tutorial_binary), "--gpu"], capture_output=True, text=True)
