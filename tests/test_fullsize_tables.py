@@ -1,7 +1,8 @@
 """The front end at benchmark size, on the CPU: the index, output-index and
 constant tables (and the seeded inputs) the engine's front end builds for
-cotan 500x500 and for B = A^T A + A at its stated size (A 10,000 x 10,000)
-have the SHA-256 digests of the tables the reference's own ComputeUnit wrote
+cotan 500x500, for B = A^T A + A at its stated size (A 10,000 x 10,000) and
+for the Neo-Hookean Hessian of a 10 x 10 x 10 cube (5,000 tets) have the
+SHA-256 digests of the tables the reference's own ComputeUnit wrote
 for the same workloads, in its CUDA layout and in its CPU
 ComputeUnit's VecWidth(4) layout (padded, blocked tables).  The digests are
 recorded in tests/golden/reference_tables.json by
@@ -24,7 +25,7 @@ def digest(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-@pytest.mark.parametrize("name,size", [("cotan", 500), ("ata", 100)])
+@pytest.mark.parametrize("name,size", [("cotan", 500), ("ata", 100), ("neohookean", 10)])
 @pytest.mark.parametrize("layout,width", [("cuda", 0), ("cpu", 4)])
 def test_tables_equal_reference(name, size, layout, width):
     w = native.Workload(name, size, 2024, vector_width=width)
