@@ -94,6 +94,15 @@ def test_cloth200_tables_equal_reference(cloth200):
     check_tables(cloth200, "cloth_200_cuda")
 
 
+@pytest.mark.parametrize("layout,width", [("cuda", 0), ("cpu", 4)])
+def test_neohookean20_tables_equal_reference(layout, width):
+    """The Neo-Hookean Hessian of a 20 x 20 x 20 cube (40,000 tets, 1,013,229
+    nonzeros; the config-5 family at the largest size whose reference plan
+    was made here) from the engine's front end, against the reference's
+    tables in both layouts."""
+    check_tables(native.Workload("neohookean", 20, 2024, vector_width=width), f"neohookean_20_{layout}")
+
+
 @pytest.mark.parametrize("name,size", [("cotan", 500), ("cloth", 200)])
 def test_cpu_layout_tables_equal_reference(name, size):
     """The reference CPU ComputeUnit's layout (VecWidth(4): padded, blocked
