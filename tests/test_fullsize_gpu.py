@@ -94,6 +94,34 @@ def test_cloth200_tables_equal_reference(cloth200):
     check_tables(cloth200, "cloth_200_cuda")
 
 
+@pytest.mark.parametrize("name,size", [("cloth", 200), ("neohookean", 20)])
+def test_reference_cpu_code_equals_oracle_at_size(name, size, tmp_path):
+    """The reference CPU ComputeUnit's own generated code for cloth 200x200 and
+    Neo-Hookean 20^3 (kept by oracle/ref_generate.sh), built in strict mode
+    and run through its five calls, gives the oracle's results bit for bit
+    (tests/test_reference_cpu_outputs.py does the smaller cases on any host;
+    these run here, where the front end is fast)."""
+    import os
+    import shutil
+    import subprocess
+    if not ref_paths.available(name, size, "cpu"):
+        pytest.skip("the reference's generated CPU code is not present here")
+    gen = tmp_path / "gen"
+    shutil.copytree(ref_paths.gen_dir(name, size, "cpu"), gen, ignore=shutil.ignore_patterns("*.so", "ref_run_cpu"))
+    env = dict(os.environ, SYMREF_STRICT="1", NUMTHREADS="4")
+    r = subprocess.run(["sh", str(ROOT / "oracle" / "ref_paths.sh"), str(gen), "cpu"], env=env, capture_output=True,
+                       text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = tmp_path / "results.bin"
+    r = subprocess.run([str(gen / "ref_run_cpu"), str(gen), str(gen / "ref_cpu.so"), "0", "1", str(out)],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    ref = np.fromfile(out, np.float64)
+    w = native.Workload(name, size, 2024)
+    oracle = np.concatenate(ocpu.evaluate(w.plan, w.index_data, w.out_index_data, w.const_data, w.inputs))
+    assert bits_equal(ref, oracle)
+
+
 @pytest.mark.parametrize("layout,width", [("cuda", 0), ("cpu", 4)])
 def test_neohookean20_tables_equal_reference(layout, width):
     """The Neo-Hookean Hessian of a 20 x 20 x 20 cube (40,000 tets, 1,013,229
