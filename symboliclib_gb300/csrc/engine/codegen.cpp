@@ -11,6 +11,13 @@
 // without FP contraction.  Plan constants (instance counts, table offsets,
 // output slots, value sets) are literals of the source, so index arithmetic
 // folds at compile time.
+//
+// A thread takes 1, 2 or 4 work items, either tpb items apart (strided) or as
+// consecutive instances of one value set whose index and constant entries it
+// reads with vector loads from padded copies of the tables (grouped).  With
+// one value set, output rows that no kernel reads may store their results
+// straight at their final positions in the unit's result buffer (direct
+// result rows, planned by the engine at init).
 #include "codegen.hpp"
 
 #include <algorithm>
