@@ -1,8 +1,8 @@
 // Compiled executor: source generation (codegen.cpp) and run-time compilation
 // (jit.cu).  A unit's kernels are emitted as straight-line CUDA C++ - the
-// form of the reference's generated kernels (ComputeUnit.cpp:409-421), one
-// work item per thread - compiled for sm_103a by NVRTC at first use and
-// cached by source text, and launched in one of three schedules.
+// form of the reference's generated kernels (ComputeUnit.cpp:409-421), with
+// 1, 2 or 4 work items per thread - compiled for sm_103a by NVRTC at first use
+// and cached by source text, and launched in one of three schedules.
 #pragma once
 #include <cstdint>
 #include <memory>
